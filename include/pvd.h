@@ -1,0 +1,153 @@
+/*
+ * pvd.h — C ABI of the GB300 (sm_103a) voxel-dosimetry hot path.
+ *
+ * Plain pointers, sizes and status codes only: no torch or CUDA types in the
+ * signatures (`pvd_stream` is ABI-identical to `cudaStream_t`).  Every device
+ * pointer argument must point to memory of the current CUDA device.  All calls
+ * return a `pvd_status`; on failure a message is available from
+ * `pvd_last_error` (thread-local).  No call aborts, traps or exits the process.
+ *
+ * Reference interfaces these entry points replace (devhliu/PyVoxelDosimetry,
+ * paths within that project):
+ *   - pvd_plan_create / pvd_plan_set_kernel:
+ *       KernelConvolutionCalculator.__init__/_load_dose_kernel
+ *       (pyvoxeldosimetry/core/kernel_convolution.py:27-46) and
+ *       KernelFactory.get_kernel (data/dose_kernels/kernel_factory.py:37-75).
+ *   - pvd_conv_execute:
+ *       KernelConvolutionCalculator.calculate_dose_rate
+ *       (pyvoxeldosimetry/core/kernel_convolution.py:48-76), the numpy
+ *       `ifftn(fftn(A) * fftn(K, A.shape)).real` at :71-74; plus the density
+ *       hook `tissue_densities` of DoseCalculator.calculate_dose
+ *       (core/dose_calculator.py:90), which the reference accepts and ignores.
+ *   - pvd_conv_execute_weighted:
+ *       the trapezoid of ActivitySampler._trapezoid_integration
+ *       (core/activity_sampler.py:69-78) and of
+ *       KernelConvolutionCalculator.calculate_absorbed_dose
+ *       (core/kernel_convolution.py:99-104), folded into the first pass.
+ *   - pvd_tac_fit_mono / pvd_tac_fit_model:
+ *       TimeCurveFitting.fit_time_activity_curve + _calculate_accumulated_dose
+ *       (time_integration/curve_fitting.py:19-84) and
+ *       fit_time_activity_curve_advanced (curve_fitting.py:112-219).
+ *   - pvd_mc_run:
+ *       MonteCarloCalculator.calculate_dose_rate (core/monte_carlo.py:104-137).
+ */
+#ifndef PVD_H_
+#define PVD_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* pvd_stream; /* == cudaStream_t; NULL = legacy default stream */
+
+typedef enum {
+  PVD_OK = 0,
+  PVD_ERR_ARG = 1,         /* invalid argument (shape, pointer, flag) */
+  PVD_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+  PVD_ERR_OOM = 3,         /* device allocation failed */
+  PVD_ERR_TIMEOUT = 4,     /* a bounded device wait ran out */
+  PVD_ERR_NUMERIC = 5,     /* non-finite or degenerate numeric input */
+  PVD_ERR_UNSUPPORTED = 6, /* size / mode outside what the plan supports */
+  PVD_ERR_STATE = 7        /* call order violated (e.g. kernel slot not set) */
+} pvd_status;
+
+/* ------------------------------------------------------------------------ */
+/* Dose-point-kernel FFT convolution                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Convolution semantics.
+ *   PVD_MODE_LINEAR  : zero-padded linear convolution cropped to the input
+ *                      grid ("same"), kernel centred at index k//2 per axis.
+ *                      Equal to the reference operator applied to inputs
+ *                      zero-padded to P >= N+K-1 and cropped at offset k//2.
+ *   PVD_MODE_CIRCULAR: exactly the reference operator
+ *                      ifftn(fftn(A) * fftn(K, A.shape)).real: circular,
+ *                      unpadded, kernel placed at the array corner and
+ *                      truncated to the volume shape where it is larger
+ *                      (output shifted by k//2 relative to LINEAR). */
+enum { PVD_MODE_LINEAR = 0, PVD_MODE_CIRCULAR = 1 };
+
+/* pvd_plan_set_kernel flags */
+enum {
+  PVD_KERNEL_NORMALIZE = 1 /* divide the kernel by its FP64 sum (on the GPU) */
+};
+
+#define PVD_MAX_KERNELS 8
+#define PVD_MAX_TIMEPOINTS 16
+
+typedef struct {
+  int n[3];           /* volume dims, slowest..fastest (C order of the numpy array) */
+  int kmax[3];        /* largest kernel dims this plan will accept (LINEAR: sets padding) */
+  int mode;           /* PVD_MODE_* */
+  int n_kernels;      /* number of kernel slots (nuclides) sharing one forward transform */
+  int pad[3];         /* explicit FFT lengths; 0 = choose automatically */
+  int flags;          /* reserved, must be 0 */
+} pvd_conv_desc;
+
+typedef struct {
+  int n[3];
+  int p[3];           /* FFT lengths actually used */
+  int h;              /* p[2]/2+1 complex bins on the fastest axis */
+  int hs;             /* row stride (complex) of the spectral buffers */
+  int n_kernels;
+  size_t workspace_bytes;  /* device bytes owned by the plan (buffers + spectra) */
+} pvd_plan_info;
+
+typedef struct pvd_plan pvd_plan;
+
+/* Create a plan on the current device; allocates its workspace with cudaMalloc. */
+pvd_status pvd_plan_create(const pvd_conv_desc* desc, pvd_plan** out);
+
+/* Query sizes of a plan. */
+pvd_status pvd_plan_get_info(const pvd_plan* plan, pvd_plan_info* info);
+
+/* Load kernel `slot` from a host FP64 array (C order, dims k0,k1,k2).  The
+ * kernel is copied to the device, optionally normalised by its FP64 sum on the
+ * GPU, multiplied by `scale`, and transformed to the padded spectrum (FP32).
+ * Synchronous with respect to the host.  Radially symmetric kernels in LINEAR
+ * mode are stored as a real spectrum; any other kernel as a complex one. */
+pvd_status pvd_plan_set_kernel(pvd_plan* plan, int slot, const double* kernel_host,
+                               int k0, int k1, int k2, double scale, int flags);
+
+/* dose[s] = out_scale * (activity (*) kernel[s]) / rho   for every slot s.
+ *   activity_d : device float32 [n0*n1*n2]
+ *   density_d  : device float32 [n0*n1*n2] or NULL (rho == 1); voxels with
+ *                rho <= 0 (or NaN) get dose 0
+ *   dose_d     : device float32 [n_kernels][n0*n1*n2] (slot-major)
+ * Enqueued on `stream`; returns once queued. */
+pvd_status pvd_conv_execute(pvd_plan* plan, const float* activity_d, const float* density_d,
+                            float* dose_d, float out_scale, pvd_stream stream);
+
+/* As pvd_conv_execute with activity = sum_t weights[t] * activity_d[t]
+ * (t < n_act <= PVD_MAX_TIMEPOINTS), the weighted sum fused into the first
+ * pass (trapezoid time integration without an extra pass over the volume). */
+pvd_status pvd_conv_execute_weighted(pvd_plan* plan, const float* const* activity_d,
+                                     const float* weights, int n_act, const float* density_d,
+                                     float* dose_d, float out_scale, pvd_stream stream);
+
+pvd_status pvd_plan_destroy(pvd_plan* plan);
+
+/* ------------------------------------------------------------------------ */
+/* Misc                                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* Copy the calling thread's last error message into buf (NUL-terminated).
+ * Returns the status of the last failing call on this thread (PVD_OK if none). */
+pvd_status pvd_last_error(char* buf, size_t len);
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+int pvd_version(void);
+
+/* Number of kernel launches this library enqueued on this thread since the
+ * last reset (instrumentation for benchmarks; monotone, never wraps in
+ * practice). */
+uint64_t pvd_launch_count(int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PVD_H_ */

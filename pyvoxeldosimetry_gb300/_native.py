@@ -1,0 +1,105 @@
+"""ctypes binding of the C ABI declared in ``include/pvd.h``.
+
+This is the only bridge between the Python host code and the CUDA library;
+the Python layer passes raw device pointers (from torch tensors) and a
+``cudaStream_t`` handle.  Loading fails loudly: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+from . import _build
+
+PVD_OK = 0
+STATUS_NAMES = {
+    0: "PVD_OK", 1: "PVD_ERR_ARG", 2: "PVD_ERR_CUDA", 3: "PVD_ERR_OOM", 4: "PVD_ERR_TIMEOUT",
+    5: "PVD_ERR_NUMERIC", 6: "PVD_ERR_UNSUPPORTED", 7: "PVD_ERR_STATE",
+}
+PVD_MODE_LINEAR = 0
+PVD_MODE_CIRCULAR = 1
+PVD_KERNEL_NORMALIZE = 1
+PVD_MAX_KERNELS = 8
+PVD_MAX_TIMEPOINTS = 16
+
+# Every symbol include/pvd.h declares, in declaration order.
+EXPORTED_SYMBOLS = [
+    "pvd_plan_create", "pvd_plan_get_info", "pvd_plan_set_kernel", "pvd_conv_execute",
+    "pvd_conv_execute_weighted", "pvd_plan_destroy",
+    "pvd_last_error", "pvd_version", "pvd_launch_count",
+]
+
+
+class PvdError(RuntimeError):
+    """A C-ABI call returned a non-OK status."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class ConvDesc(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("kmax", C.c_int * 3), ("mode", C.c_int), ("n_kernels", C.c_int),
+                ("pad", C.c_int * 3), ("flags", C.c_int)]
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("p", C.c_int * 3), ("h", C.c_int), ("hs", C.c_int),
+                ("n_kernels", C.c_int), ("workspace_bytes", C.c_size_t)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib_path() -> Path:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load ``libpvd_gb300.so`` (building it first if it is missing or stale)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if build_if_missing and _build.needs_build():
+            _build.build()
+        path = _build.LIB_PATH
+        if not path.exists():
+            raise RuntimeError(f"{path} is missing; run pyvoxeldosimetry_gb300._build.build()")
+        lib = C.CDLL(str(path))
+        _declare(lib)
+        _lib = lib
+        return lib
+
+
+def _declare(lib: C.CDLL) -> None:
+    vp, i, f, d, st = C.c_void_p, C.c_int, C.c_float, C.c_double, C.c_int
+    sig = {
+        "pvd_plan_create": (st, [C.POINTER(ConvDesc), C.POINTER(vp)]),
+        "pvd_plan_get_info": (st, [vp, C.POINTER(PlanInfo)]),
+        "pvd_plan_set_kernel": (st, [vp, i, vp, i, i, i, d, i]),
+        "pvd_conv_execute": (st, [vp, vp, vp, vp, f, vp]),
+        "pvd_conv_execute_weighted": (st, [vp, vp, vp, i, vp, vp, f, vp]),
+        "pvd_plan_destroy": (st, [vp]),
+        "pvd_last_error": (st, [C.c_char_p, C.c_size_t]),
+        "pvd_version": (i, []),
+        "pvd_launch_count": (C.c_uint64, [i]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def last_error() -> str:
+    lib = load()
+    buf = C.create_string_buffer(1024)
+    lib.pvd_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(status: int) -> None:
+    if status != PVD_OK:
+        raise PvdError(status, last_error())

@@ -1,0 +1,744 @@
+// Dose-point-kernel convolution as a pruned, fused 3D real FFT pipeline.
+//
+// Replaces the reference operator
+//   np.fft.ifftn(np.fft.fftn(A) * np.fft.fftn(K, A.shape)).real
+// (pyvoxeldosimetry/core/kernel_convolution.py:71-74) with five passes over
+// HBM, each a batch of 1D mixed-radix (2,3,4,5,7,8) Stockham FFTs done in
+// shared memory:
+//
+//   pass 1  x  : weighted sum of timepoints -> zero-pad -> R2C      act  -> B1[N0][N1][HS]
+//   pass 2  y  : zero-pad -> C2C forward                            B1   -> B2[N0][P1][HS]
+//   pass 3  z  : zero-pad -> C2C forward -> * S_k -> C2C inverse     B2   -> B3_k[N0][P1][HS]
+//                -> crop     (one forward, one multiply+inverse per kernel slot k)
+//   pass 4  y  : C2C inverse -> crop                                B3_k -> B1[N0][N1][HS]
+//   pass 5  x  : C2R -> crop -> * out_scale / rho                   B1   -> dose_k[N0][N1][N2]
+//
+// Axis 2 (x) is the contiguous axis of the C-ordered volume.  Zero padding is
+// never materialised: rows that are all zero are skipped (pruned) and the pad
+// region of each transform is filled in shared memory.  Two real rows are
+// packed into one complex transform on the x axis.
+//
+// Kernel placement: LINEAR mode puts kernel index m at padded index
+// (m - k//2) mod P (kernel centred at the origin) so the output needs no shift
+// and a symmetric kernel has a real spectrum; CIRCULAR mode puts it at m
+// (the reference's corner placement, truncated to P) which reproduces the
+// reference's K//2 output shift exactly.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pvd_common.cuh"
+
+namespace pvd {
+
+constexpr int TX = 16;        // transforms (columns) per CTA
+constexpr int TXP = TX + 1;   // padded shared-memory row stride (complex)
+constexpr int NT = 256;       // threads per CTA
+constexpr int NL = NT / TX;   // lanes per transform
+constexpr int MAX_STAGES = 16;
+
+struct FftLen {
+  int L;
+  int nst;
+  int rad[MAX_STAGES];
+};
+
+struct ActIn {
+  const float* p[PVD_MAX_TIMEPOINTS];
+  float w[PVD_MAX_TIMEPOINTS];
+  int n;
+};
+
+struct OutSet {
+  float2* p[PVD_MAX_KERNELS];
+  const void* s[PVD_MAX_KERNELS];
+  int real[PVD_MAX_KERNELS];
+  int n;
+};
+
+// ---------------------------------------------------------------------------
+// host-side length helpers
+// ---------------------------------------------------------------------------
+static bool factorize(int L, FftLen* f) {
+  f->L = L;
+  f->nst = 0;
+  int r = L;
+  std::vector<int> rad;
+  while (r % 8 == 0) { rad.push_back(8); r /= 8; }
+  while (r % 4 == 0) { rad.push_back(4); r /= 4; }
+  while (r % 2 == 0) { rad.push_back(2); r /= 2; }
+  while (r % 3 == 0) { rad.push_back(3); r /= 3; }
+  while (r % 5 == 0) { rad.push_back(5); r /= 5; }
+  while (r % 7 == 0) { rad.push_back(7); r /= 7; }
+  if (r != 1 || (int)rad.size() > MAX_STAGES) return false;
+  for (size_t i = 0; i < rad.size(); ++i) f->rad[i] = rad[i];
+  f->nst = (int)rad.size();
+  return true;
+}
+
+static bool is_smooth7(int n) {
+  if (n < 1) return false;
+  for (int p : {2, 3, 5, 7})
+    while (n % p == 0) n /= p;
+  return n == 1;
+}
+
+static int next_smooth7(int n) {
+  int m = std::max(n, 1);
+  while (!is_smooth7(m)) ++m;
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// device: Stockham stage and tile FFT along the row index of a [L][TXP] tile
+// ---------------------------------------------------------------------------
+template <int R, bool INV>
+__device__ __forceinline__ void stockham_stage(const float2* __restrict__ a, float2* __restrict__ b, int L, int ns,
+                                               const float2* __restrict__ tw, int col, int lane) {
+  const int m = L / R;
+  const int tstep = L / (ns * R);
+  for (int j = lane; j < m; j += NL) {
+    const int k = j % ns;
+    float2 v[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) v[q] = a[(j + q * m) * TXP + col];
+    if (ns > 1) {
+#pragma unroll
+      for (int q = 1; q < R; ++q) {
+        float2 w = tw[q * k * tstep];
+        if (INV) w.y = -w.y;
+        v[q] = cmul(v[q], w);
+      }
+    }
+    Dft<R, INV>::run(v);
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int q = 0; q < R; ++q) b[(base + q * ns) * TXP + col] = v[q];
+  }
+}
+
+// FFT of TX columns of length f.L held in `a`; ping-pongs with `b`; returns
+// the buffer holding the natural-order result.  Caller syncs before the call.
+template <bool INV>
+__device__ float2* fft_tile(float2* a, float2* b, const FftLen& f, const float2* tw) {
+  const int col = threadIdx.x % TX;
+  const int lane = threadIdx.x / TX;
+  int ns = 1;
+  for (int s = 0; s < f.nst; ++s) {
+    const int r = f.rad[s];
+    switch (r) {
+      case 2: stockham_stage<2, INV>(a, b, f.L, ns, tw, col, lane); break;
+      case 3: stockham_stage<3, INV>(a, b, f.L, ns, tw, col, lane); break;
+      case 4: stockham_stage<4, INV>(a, b, f.L, ns, tw, col, lane); break;
+      case 5: stockham_stage<5, INV>(a, b, f.L, ns, tw, col, lane); break;
+      case 7: stockham_stage<7, INV>(a, b, f.L, ns, tw, col, lane); break;
+      default: stockham_stage<8, INV>(a, b, f.L, ns, tw, col, lane); break;
+    }
+    __syncthreads();
+    float2* t = a;
+    a = b;
+    b = t;
+    ns *= r;
+  }
+  return a;
+}
+
+__device__ __forceinline__ void load_twiddles(float2* tw_s, const float2* __restrict__ tw_g, int L) {
+  for (int i = threadIdx.x; i < L; i += NT) tw_s[i] = tw_g[i];
+}
+
+// ---------------------------------------------------------------------------
+// pass 1: x-axis forward R2C of pairs of real rows (weighted timepoint sum)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(NT) k_x_fwd(ActIn in, float2* __restrict__ out, int nrows, int N2, int HS, FftLen f,
+                                              const float2* __restrict__ twg) {
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* a = sm + f.L;
+  float2* b = a + f.L * TXP;
+  load_twiddles(tw, twg, f.L);
+  const long long row0 = (long long)blockIdx.x * (2 * TX);
+  for (int idx = threadIdx.x; idx < TX * f.L; idx += NT) {
+    const int m = idx / f.L, n = idx - (idx / f.L) * f.L;
+    float2 v = make_float2(0.f, 0.f);
+    if (n < N2) {
+      const long long ra = row0 + 2 * m, rb = ra + 1;
+      if (ra < nrows) {
+        const long long o = ra * N2 + n;
+        float s = 0.f;
+        for (int t = 0; t < in.n; ++t) s += in.w[t] * __ldg(in.p[t] + o);
+        v.x = s;
+      }
+      if (rb < nrows) {
+        const long long o = rb * N2 + n;
+        float s = 0.f;
+        for (int t = 0; t < in.n; ++t) s += in.w[t] * __ldg(in.p[t] + o);
+        v.y = s;
+      }
+    }
+    a[n * TXP + m] = v;
+  }
+  __syncthreads();
+  float2* r = fft_tile<false>(a, b, f, tw);
+  const int H = f.L / 2 + 1;
+  for (int idx = threadIdx.x; idx < TX * H; idx += NT) {
+    const int m = idx / H, k = idx - (idx / H) * H;
+    const long long ra = row0 + 2 * m, rb = ra + 1;
+    const int kk = (k == 0) ? 0 : f.L - k;
+    const float2 z1 = r[k * TXP + m];
+    const float2 z2 = r[kk * TXP + m];
+    // Xa = (Z[k] + conj Z[-k]) / 2 ;  Xb = (Z[k] - conj Z[-k]) / (2i)
+    const float2 xa = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+    const float2 xb = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
+    if (ra < nrows) out[ra * HS + k] = xa;
+    if (rb < nrows) out[rb * HS + k] = xb;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// passes 2 and 4: y-axis C2C over columns, zero-pad input rows >= nin, keep
+// output rows < nout.  blockIdx.x: column tile, blockIdx.y: z slab.
+// ---------------------------------------------------------------------------
+template <bool INV>
+__global__ void __launch_bounds__(NT) k_y(const float2* __restrict__ in, float2* __restrict__ out, int nin, int nout,
+                                          int HS, FftLen f, const float2* __restrict__ twg) {
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* a = sm + f.L;
+  float2* b = a + f.L * TXP;
+  load_twiddles(tw, twg, f.L);
+  const int kx0 = blockIdx.x * TX;
+  const float2* src = in + (long long)blockIdx.y * nin * HS + kx0;
+  float2* dst = out + (long long)blockIdx.y * nout * HS + kx0;
+  for (int idx = threadIdx.x; idx < TX * f.L; idx += NT) {
+    const int n = idx / TX, c = idx % TX;
+    a[n * TXP + c] = (n < nin) ? src[(long long)n * HS + c] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  float2* r = fft_tile<INV>(a, b, f, tw);
+  for (int idx = threadIdx.x; idx < TX * nout; idx += NT) {
+    const int n = idx / TX, c = idx % TX;
+    dst[(long long)n * HS + c] = r[n * TXP + c];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pass 3: z-axis forward, spectrum multiply, inverse, crop — per kernel slot.
+// in:  [N0][P1][HS] (rows z < N0 valid);  out_k: [N0][P1][HS].
+// blockIdx.x: column tile, blockIdx.y: ky.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(NT) k_z(const float2* __restrict__ in, OutSet os, int N0, int P1, int HS, FftLen f,
+                                          const float2* __restrict__ twg) {
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* bufs[3];
+  bufs[0] = sm + f.L;
+  bufs[1] = bufs[0] + f.L * TXP;
+  bufs[2] = bufs[1] + f.L * TXP;
+  load_twiddles(tw, twg, f.L);
+  const int kx0 = blockIdx.x * TX;
+  const int ky = blockIdx.y;
+  const long long zstride = (long long)P1 * HS;
+  const long long base = (long long)ky * HS + kx0;
+  for (int idx = threadIdx.x; idx < TX * f.L; idx += NT) {
+    const int z = idx / TX, c = idx % TX;
+    bufs[0][z * TXP + c] = (z < N0) ? in[z * zstride + base + c] : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  float2* X = fft_tile<false>(bufs[0], bufs[1], f, tw);
+  const int xi = (X == bufs[0]) ? 0 : 1;
+  for (int s = 0; s < os.n; ++s) {
+    float2* A;
+    float2* B;
+    if (os.n == 1) {
+      A = X;
+      B = bufs[1 - xi];
+    } else {
+      A = bufs[1 - xi];
+      B = bufs[2];
+    }
+    const long long sbase = (long long)ky * HS + kx0;
+    if (os.real[s]) {
+      const float* S = (const float*)os.s[s];
+      for (int idx = threadIdx.x; idx < TX * f.L; idx += NT) {
+        const int z = idx / TX, c = idx % TX;
+        A[z * TXP + c] = cscale(X[z * TXP + c], __ldg(S + z * zstride + sbase + c));
+      }
+    } else {
+      const float2* S = (const float2*)os.s[s];
+      for (int idx = threadIdx.x; idx < TX * f.L; idx += NT) {
+        const int z = idx / TX, c = idx % TX;
+        A[z * TXP + c] = cmul(X[z * TXP + c], __ldg(S + z * zstride + sbase + c));
+      }
+    }
+    __syncthreads();
+    float2* r = fft_tile<true>(A, B, f, tw);
+    float2* dst = os.p[s];
+    for (int idx = threadIdx.x; idx < TX * N0; idx += NT) {
+      const int z = idx / TX, c = idx % TX;
+      dst[z * zstride + base + c] = r[z * TXP + c];
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pass 5: x-axis inverse C2R of pairs of rows, crop, scale, density.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(NT) k_x_inv(const float2* __restrict__ in, float* __restrict__ out,
+                                              const float* __restrict__ rho, int nrows, int N2, int HS, float scale,
+                                              FftLen f, const float2* __restrict__ twg) {
+  extern __shared__ float2 sm[];
+  float2* tw = sm;
+  float2* a = sm + f.L;
+  float2* b = a + f.L * TXP;
+  load_twiddles(tw, twg, f.L);
+  const long long row0 = (long long)blockIdx.x * (2 * TX);
+  const int H = f.L / 2 + 1;
+  for (int idx = threadIdx.x; idx < TX * H; idx += NT) {
+    const int m = idx / H, k = idx - (idx / H) * H;
+    const long long ra = row0 + 2 * m, rb = ra + 1;
+    float2 xa = (ra < nrows) ? in[ra * HS + k] : make_float2(0.f, 0.f);
+    float2 xb = (rb < nrows) ? in[rb * HS + k] : make_float2(0.f, 0.f);
+    if (k == 0 || 2 * k == f.L) {  // DC / Nyquist bins of a real row are real
+      xa.y = 0.f;
+      xb.y = 0.f;
+    }
+    a[k * TXP + m] = make_float2(xa.x - xb.y, xa.y + xb.x);  // Xa + i Xb
+    const int kk = f.L - k;
+    if (k > 0 && kk >= H) a[kk * TXP + m] = make_float2(xa.x + xb.y, xb.x - xa.y);  // conj Xa + i conj Xb
+  }
+  __syncthreads();
+  float2* r = fft_tile<true>(a, b, f, tw);
+  for (int idx = threadIdx.x; idx < TX * N2; idx += NT) {
+    const int m = idx / N2, n = idx - (idx / N2) * N2;
+    const long long ra = row0 + 2 * m, rb = ra + 1;
+    const float2 z = r[n * TXP + m];
+    if (ra < nrows) {
+      float v = z.x * scale;
+      if (rho) {
+        const float d = __ldg(rho + ra * N2 + n);
+        v = (d > 0.f) ? v / d : 0.f;
+      }
+      out[ra * N2 + n] = v;
+    }
+    if (rb < nrows) {
+      float v = z.y * scale;
+      if (rho) {
+        const float d = __ldg(rho + rb * N2 + n);
+        v = (d > 0.f) ? v / d : 0.f;
+      }
+      out[rb * N2 + n] = v;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// kernel spectrum: FP64 normalisation sum, scale, and a separable direct DFT
+// of the (small) placed kernel into the padded spectral layout.
+// ---------------------------------------------------------------------------
+__global__ void k_sum_f64(const double* __restrict__ k, long long n, double* __restrict__ out) {
+  __shared__ double red[NT];
+  double s = 0.0;
+  for (long long i = threadIdx.x; i < n; i += NT) s += k[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = NT / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// kf = float(k * factor) where factor = scale / sum (or scale) / (P0 P1 P2), all FP64
+__global__ void k_scale_to_f32(const double* __restrict__ k, long long n, const double* __restrict__ sum,
+                               double scale_over_p, float* __restrict__ kf) {
+  const double fac = sum ? scale_over_p / *sum : scale_over_p;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    kf[i] = (float)(k[i] * fac);
+}
+
+// T1[m0][m1][kx] = sum_m2 k[m0][m1][m2] w2^(kx * ((m2 - o2) mod P2))
+__global__ void k_spec_x(const float* __restrict__ kf, float2* __restrict__ t1, int K0, int K1, int K2, int K2e,
+                         int o2, int P2, int H, const float2* __restrict__ tw2) {
+  const long long total = (long long)K0 * K1 * H;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % H);
+    const long long row = i / H;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int m = 0; m < K2e; ++m) {
+      const int p = ((m - o2) % P2 + P2) % P2;
+      const float v = kf[row * K2 + m];
+      const float2 w = tw2[(int)(((long long)kx * p) % P2)];
+      acc.x += v * w.x;
+      acc.y += v * w.y;
+    }
+    t1[i] = acc;
+  }
+}
+
+// T2[m0][ky][kx] = sum_m1 T1[m0][m1][kx] w1^(ky * ((m1 - o1) mod P1))
+__global__ void k_spec_y(const float2* __restrict__ t1, float2* __restrict__ t2, int K0, int K1, int K1e, int o1,
+                         int P1, int H, const float2* __restrict__ tw1) {
+  const long long total = (long long)K0 * P1 * H;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % H);
+    const int ky = (int)((i / H) % P1);
+    const int m0 = (int)(i / ((long long)H * P1));
+    float2 acc = make_float2(0.f, 0.f);
+    for (int m = 0; m < K1e; ++m) {
+      const int p = ((m - o1) % P1 + P1) % P1;
+      const float2 v = t1[((long long)m0 * K1 + m) * H + kx];
+      acc = cadd(acc, cmul(v, tw1[(int)(((long long)ky * p) % P1)]));
+    }
+    t2[i] = acc;
+  }
+}
+
+// S[kz][ky][kx] = sum_m0 T2[m0][ky][kx] w0^(kz * ((m0 - o0) mod P0)); kx in [H, HS) -> 0
+__global__ void k_spec_z(const float2* __restrict__ t2, void* __restrict__ spec, int real_out, int K0e, int o0,
+                         int P0, int P1, int H, int HS, const float2* __restrict__ tw0) {
+  const long long total = (long long)P0 * P1 * HS;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(i % HS);
+    const int ky = (int)((i / HS) % P1);
+    const int kz = (int)(i / ((long long)HS * P1));
+    float2 acc = make_float2(0.f, 0.f);
+    if (kx < H) {
+      for (int m = 0; m < K0e; ++m) {
+        const int p = ((m - o0) % P0 + P0) % P0;
+        const float2 v = t2[((long long)m * P1 + ky) * H + kx];
+        acc = cadd(acc, cmul(v, tw0[(int)(((long long)kz * p) % P0)]));
+      }
+    }
+    if (real_out)
+      ((float*)spec)[i] = acc.x;
+    else
+      ((float2*)spec)[i] = acc;
+  }
+}
+
+}  // namespace pvd
+
+// ===========================================================================
+// plan object and C ABI
+// ===========================================================================
+using namespace pvd;
+
+struct pvd_plan {
+  int dev = 0;
+  int mode = PVD_MODE_LINEAR;
+  int N[3] = {0, 0, 0};
+  int P[3] = {0, 0, 0};
+  int kmax[3] = {0, 0, 0};
+  int H = 0, HS = 0, nk = 0;
+  FftLen f[3];
+  float2* tw[3] = {nullptr, nullptr, nullptr};
+  float2* buf1 = nullptr;
+  float2* buf2 = nullptr;
+  float2* buf3[PVD_MAX_KERNELS] = {};
+  void* spec[PVD_MAX_KERNELS] = {};
+  int spec_real[PVD_MAX_KERNELS] = {};
+  int spec_set[PVD_MAX_KERNELS] = {};
+  size_t ws_bytes = 0;
+  size_t smem_x = 0, smem_y = 0, smem_z = 0;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+pvd_status plan_alloc(pvd_plan* p, size_t bytes, void** out) {
+  void* ptr = nullptr;
+  cudaError_t e = cudaMalloc(&ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return cuda_error(e, "cudaMalloc(plan workspace)");
+  }
+  p->allocs.push_back(ptr);
+  p->ws_bytes += bytes;
+  *out = ptr;
+  return PVD_OK;
+}
+
+void plan_free(pvd_plan* p) {
+  for (void* a : p->allocs) cudaFree(a);
+  p->allocs.clear();
+}
+
+size_t smem_bytes(int L, int nbuf) { return (size_t)(L + nbuf * L * TXP) * sizeof(float2); }
+
+}  // namespace
+
+extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
+  if (!d || !out) return set_error(PVD_ERR_ARG, "pvd_plan_create: null argument");
+  *out = nullptr;
+  if (d->flags != 0) return set_error(PVD_ERR_ARG, "pvd_plan_create: flags must be 0");
+  if (d->mode != PVD_MODE_LINEAR && d->mode != PVD_MODE_CIRCULAR)
+    return set_error(PVD_ERR_ARG, "pvd_plan_create: unknown mode");
+  if (d->n_kernels < 1 || d->n_kernels > PVD_MAX_KERNELS)
+    return set_error(PVD_ERR_ARG, "pvd_plan_create: n_kernels must be in [1, 8]");
+  for (int i = 0; i < 3; ++i) {
+    if (d->n[i] < 1 || d->n[i] > 4096) return set_error(PVD_ERR_ARG, "pvd_plan_create: volume dims must be in [1, 4096]");
+    if (d->mode == PVD_MODE_LINEAR && (d->kmax[i] < 1 || d->kmax[i] > 1024))
+      return set_error(PVD_ERR_ARG, "pvd_plan_create: kmax must be in [1, 1024] for LINEAR mode");
+  }
+  pvd_plan* p = new pvd_plan();
+  p->mode = d->mode;
+  p->nk = d->n_kernels;
+  cudaGetDevice(&p->dev);
+  for (int i = 0; i < 3; ++i) {
+    p->N[i] = d->n[i];
+    p->kmax[i] = d->kmax[i];
+    int need = (d->mode == PVD_MODE_LINEAR) ? d->n[i] + d->kmax[i] - 1 : d->n[i];
+    int L = d->pad[i] ? d->pad[i] : (d->mode == PVD_MODE_LINEAR ? next_smooth7(need) : need);
+    if (L < need || (d->mode == PVD_MODE_CIRCULAR && L != need)) {
+      delete p;
+      return set_error(PVD_ERR_ARG, "pvd_plan_create: explicit pad too small (LINEAR needs n+kmax-1, CIRCULAR needs n)");
+    }
+    if (!factorize(L, &p->f[i])) {
+      delete p;
+      return set_error(PVD_ERR_UNSUPPORTED, "pvd_plan_create: FFT length " + std::to_string(L) +
+                                                " has a prime factor > 7 (CIRCULAR mode needs 7-smooth dims)");
+    }
+    p->P[i] = L;
+  }
+  p->H = p->P[2] / 2 + 1;
+  p->HS = (p->H + TX - 1) / TX * TX;
+  p->smem_x = smem_bytes(p->P[2], 2);
+  p->smem_y = smem_bytes(p->P[1], 2);
+  p->smem_z = smem_bytes(p->P[0], p->nk > 1 ? 3 : 2);
+  int smem_max = 0;
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->dev);
+  if ((int)std::max({p->smem_x, p->smem_y, p->smem_z}) > smem_max) {
+    delete p;
+    return set_error(PVD_ERR_UNSUPPORTED, "pvd_plan_create: FFT length too large for one shared-memory tile");
+  }
+  cudaFuncSetAttribute(k_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute(k_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute(k_y<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute(k_y<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute(k_z, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+
+  pvd_status st = PVD_OK;
+  // twiddle tables exp(-2 pi i n / L), computed in FP64 on the host
+  for (int i = 0; i < 3 && st == PVD_OK; ++i) {
+    int L = p->P[i];
+    std::vector<float2> h(L);
+    for (int n = 0; n < L; ++n) {
+      double a = -2.0 * M_PI * (double)n / (double)L;
+      h[n] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    void* ptr = nullptr;
+    st = plan_alloc(p, sizeof(float2) * L, &ptr);
+    if (st == PVD_OK) {
+      p->tw[i] = (float2*)ptr;
+      cudaError_t e = cudaMemcpy(ptr, h.data(), sizeof(float2) * L, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) st = cuda_error(e, "cudaMemcpy(twiddles)");
+    }
+  }
+  const size_t b1 = sizeof(float2) * (size_t)p->N[0] * p->N[1] * p->HS;
+  const size_t b2 = sizeof(float2) * (size_t)p->N[0] * p->P[1] * p->HS;
+  const size_t sp = (size_t)p->P[0] * p->P[1] * p->HS;
+  void* ptr = nullptr;
+  if (st == PVD_OK) st = plan_alloc(p, b1, &ptr), p->buf1 = (float2*)ptr;
+  if (st == PVD_OK) st = plan_alloc(p, b2, &ptr), p->buf2 = (float2*)ptr;
+  if (st == PVD_OK) p->buf3[0] = p->buf2;  // slot 0 transforms in place
+  for (int s = 1; s < p->nk && st == PVD_OK; ++s) st = plan_alloc(p, b2, &ptr), p->buf3[s] = (float2*)ptr;
+  for (int s = 0; s < p->nk && st == PVD_OK; ++s) st = plan_alloc(p, sizeof(float2) * sp, &ptr), p->spec[s] = ptr;
+  if (st == PVD_OK) {
+    // padding columns [H, HS) are carried through the column passes; keep them defined
+    cudaError_t e = cudaMemset(p->buf1, 0, b1);
+    if (e == cudaSuccess) e = cudaMemset(p->buf2, 0, b2);
+    for (int s = 1; s < p->nk && e == cudaSuccess; ++s) e = cudaMemset(p->buf3[s], 0, b2);
+    if (e != cudaSuccess) st = cuda_error(e, "cudaMemset(workspace)");
+  }
+  if (st != PVD_OK) {
+    plan_free(p);
+    delete p;
+    return st;
+  }
+  *out = p;
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_plan_get_info(const pvd_plan* p, pvd_plan_info* info) {
+  if (!p || !info) return set_error(PVD_ERR_ARG, "pvd_plan_get_info: null argument");
+  for (int i = 0; i < 3; ++i) {
+    info->n[i] = p->N[i];
+    info->p[i] = p->P[i];
+  }
+  info->h = p->H;
+  info->hs = p->HS;
+  info->n_kernels = p->nk;
+  info->workspace_bytes = p->ws_bytes;
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_plan_set_kernel(pvd_plan* p, int slot, const double* kh, int k0, int k1, int k2,
+                                          double scale, int flags) {
+  if (!p || !kh) return set_error(PVD_ERR_ARG, "pvd_plan_set_kernel: null argument");
+  if (slot < 0 || slot >= p->nk) return set_error(PVD_ERR_ARG, "pvd_plan_set_kernel: slot out of range");
+  if (flags & ~PVD_KERNEL_NORMALIZE) return set_error(PVD_ERR_ARG, "pvd_plan_set_kernel: unknown flags");
+  const int K[3] = {k0, k1, k2};
+  for (int i = 0; i < 3; ++i) {
+    if (K[i] < 1) return set_error(PVD_ERR_ARG, "pvd_plan_set_kernel: kernel dims must be >= 1");
+    if (p->mode == PVD_MODE_LINEAR && K[i] > p->kmax[i])
+      return set_error(PVD_ERR_ARG, "pvd_plan_set_kernel: kernel larger than the plan's kmax");
+  }
+  if (!std::isfinite(scale)) return set_error(PVD_ERR_NUMERIC, "pvd_plan_set_kernel: non-finite scale");
+  const long long nk = (long long)k0 * k1 * k2;
+  for (long long i = 0; i < nk; ++i)
+    if (!std::isfinite(kh[i]))
+      return set_error(PVD_ERR_NUMERIC, "pvd_plan_set_kernel: kernel has a non-finite value at flat index " +
+                                            std::to_string(i));
+  // placement offsets and symmetry (real spectrum) detection
+  int o[3], Ke[3];
+  bool sym = (p->mode == PVD_MODE_LINEAR);
+  for (int i = 0; i < 3; ++i) {
+    o[i] = (p->mode == PVD_MODE_LINEAR) ? K[i] / 2 : 0;
+    Ke[i] = std::min(K[i], p->P[i]);
+    if (K[i] % 2 == 0) sym = false;
+  }
+  for (long long i = 0; sym && i < nk; ++i) {
+    const int a = (int)(i / ((long long)k1 * k2)), b = (int)((i / k2) % k1), c = (int)(i % k2);
+    const long long j = ((long long)(k0 - 1 - a) * k1 + (k1 - 1 - b)) * k2 + (k2 - 1 - c);
+    if (kh[i] != kh[j]) sym = false;
+  }
+  const double inv_p = 1.0 / ((double)p->P[0] * p->P[1] * p->P[2]);
+
+  double* kd = nullptr;
+  double* sumd = nullptr;
+  float* kf = nullptr;
+  float2* t1 = nullptr;
+  float2* t2 = nullptr;
+  pvd_status st = PVD_OK;
+  auto cleanup = [&]() {
+    cudaFree(kd);
+    cudaFree(sumd);
+    cudaFree(kf);
+    cudaFree(t1);
+    cudaFree(t2);
+  };
+  cudaError_t e = cudaMalloc(&kd, sizeof(double) * nk);
+  if (e == cudaSuccess) e = cudaMalloc(&sumd, sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&kf, sizeof(float) * nk);
+  if (e == cudaSuccess) e = cudaMalloc(&t1, sizeof(float2) * (size_t)k0 * k1 * p->H);
+  if (e == cudaSuccess) e = cudaMalloc(&t2, sizeof(float2) * (size_t)k0 * p->P[1] * p->H);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cleanup();
+    return cuda_error(e, "cudaMalloc(kernel staging)");
+  }
+  e = cudaMemcpy(kd, kh, sizeof(double) * nk, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cleanup();
+    return cuda_error(e, "cudaMemcpy(kernel)");
+  }
+  const bool norm = (flags & PVD_KERNEL_NORMALIZE) != 0;
+  if (norm) {
+    k_sum_f64<<<1, NT>>>(kd, nk, sumd);
+    count_launch();
+    double hsum = 0.0;
+    e = cudaMemcpy(&hsum, sumd, sizeof(double), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+      cleanup();
+      return cuda_error(e, "k_sum_f64");
+    }
+    if (!(std::isfinite(hsum) && hsum != 0.0)) {
+      cleanup();
+      return set_error(PVD_ERR_NUMERIC, "pvd_plan_set_kernel: kernel sum is zero or non-finite; cannot normalise");
+    }
+  }
+  const int gs = 152 * 8;
+  k_scale_to_f32<<<gs, NT>>>(kd, nk, norm ? sumd : nullptr, scale * inv_p, kf);
+  count_launch();
+  k_spec_x<<<gs, NT>>>(kf, t1, k0, k1, k2, Ke[2], o[2], p->P[2], p->H, p->tw[2]);
+  count_launch();
+  k_spec_y<<<gs, NT>>>(t1, t2, k0, k1, Ke[1], o[1], p->P[1], p->H, p->tw[1]);
+  count_launch();
+  k_spec_z<<<gs, NT>>>(t2, p->spec[slot], sym ? 1 : 0, Ke[0], o[0], p->P[0], p->P[1], p->H, p->HS, p->tw[0]);
+  count_launch();
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) st = cuda_error(e, "kernel spectrum");
+  cleanup();
+  if (st == PVD_OK) {
+    p->spec_real[slot] = sym ? 1 : 0;
+    p->spec_set[slot] = 1;
+  }
+  return st;
+}
+
+static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float* dose, float out_scale,
+                           pvd_stream stream) {
+  for (int s = 0; s < p->nk; ++s)
+    if (!p->spec_set[s]) return set_error(PVD_ERR_STATE, "pvd_conv_execute: kernel slot " + std::to_string(s) + " not set");
+  if (!dose) return set_error(PVD_ERR_ARG, "pvd_conv_execute: null dose pointer");
+  if (!std::isfinite(out_scale)) return set_error(PVD_ERR_NUMERIC, "pvd_conv_execute: non-finite out_scale");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N0 = p->N[0], N1 = p->N[1], N2 = p->N[2];
+  const int nrows = N0 * N1;
+  const long long vox = (long long)nrows * N2;
+  const int xblocks = (nrows + 2 * TX - 1) / (2 * TX);
+  const int ctiles = p->HS / TX;
+
+  k_x_fwd<<<xblocks, NT, p->smem_x, st>>>(in, p->buf1, nrows, N2, p->HS, p->f[2], p->tw[2]);
+  PVD_LAUNCH_CHECK("k_x_fwd");
+  k_y<false><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf1, p->buf2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
+  PVD_LAUNCH_CHECK("k_y<fwd>");
+  OutSet os;
+  std::memset(&os, 0, sizeof(os));
+  os.n = p->nk;
+  for (int s = 0; s < p->nk; ++s) {
+    os.p[s] = p->buf3[s];
+    os.s[s] = p->spec[s];
+    os.real[s] = p->spec_real[s];
+  }
+  k_z<<<dim3(ctiles, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
+  PVD_LAUNCH_CHECK("k_z");
+  for (int s = 0; s < p->nk; ++s) {
+    k_y<true><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS, p->f[1], p->tw[1]);
+    PVD_LAUNCH_CHECK("k_y<inv>");
+    k_x_inv<<<xblocks, NT, p->smem_x, st>>>(p->buf1, dose + s * vox, rho, nrows, N2, p->HS, out_scale, p->f[2],
+                                           p->tw[2]);
+    PVD_LAUNCH_CHECK("k_x_inv");
+  }
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_conv_execute(pvd_plan* p, const float* act, const float* rho, float* dose, float out_scale,
+                                       pvd_stream stream) {
+  if (!p || !act) return set_error(PVD_ERR_ARG, "pvd_conv_execute: null argument");
+  ActIn in;
+  std::memset(&in, 0, sizeof(in));
+  in.n = 1;
+  in.p[0] = act;
+  in.w[0] = 1.0f;
+  return conv_run(p, in, rho, dose, out_scale, stream);
+}
+
+extern "C" pvd_status pvd_conv_execute_weighted(pvd_plan* p, const float* const* act, const float* w, int n_act,
+                                                const float* rho, float* dose, float out_scale, pvd_stream stream) {
+  if (!p || !act || !w) return set_error(PVD_ERR_ARG, "pvd_conv_execute_weighted: null argument");
+  if (n_act < 1 || n_act > PVD_MAX_TIMEPOINTS)
+    return set_error(PVD_ERR_ARG, "pvd_conv_execute_weighted: n_act must be in [1, 16]");
+  ActIn in;
+  std::memset(&in, 0, sizeof(in));
+  in.n = n_act;
+  for (int t = 0; t < n_act; ++t) {
+    if (!act[t]) return set_error(PVD_ERR_ARG, "pvd_conv_execute_weighted: null activity pointer");
+    if (!std::isfinite(w[t])) return set_error(PVD_ERR_NUMERIC, "pvd_conv_execute_weighted: non-finite weight");
+    in.p[t] = act[t];
+    in.w[t] = w[t];
+  }
+  return conv_run(p, in, rho, dose, out_scale, stream);
+}
+
+extern "C" pvd_status pvd_plan_destroy(pvd_plan* p) {
+  if (!p) return PVD_OK;
+  plan_free(p);
+  delete p;
+  return PVD_OK;
+}

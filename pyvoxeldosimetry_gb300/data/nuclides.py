@@ -1,0 +1,185 @@
+"""Radionuclide data and dose-point-kernel builders (host, FP64).
+
+Nuclide constants restate the reference's data files (paths within
+devhliu/PyVoxelDosimetry):
+  Y90  : data/dose_kernels/Y90/Y90.json:16-23 (T1/2 64.1 h, Emax 2.280, Emean 0.934 MeV);
+         data/mc_decay/Y90.json:5-19 (beta spectrum points)
+  Lu177: data/mc_decay/Lu177.json:5-32 (T1/2 6.647 d, Emean 0.149, Emax 0.498 MeV, gammas);
+         data/dose_kernels/Lu177/Lu177.json:21-26 (beta branches, used by the reference generator)
+  I131 : data/mc_decay/I131.json:5-38 (T1/2 8.0207 d, Emean 0.182, Emax 0.807 MeV, gammas)
+  F18, Ga68, Tb161: data/dose_kernels/*/ *.json "half_life" and mean/max energies.
+
+Kernel profiles:
+  "analytic"  : k(r) = exp(-r/lambda)/r^2, lambda = 1.8 mm for Y-90 and scaled by the
+                nuclide's beta CSDA range (data/mc_decay/*.json "beta_csda_range") for
+                the others; the centre voxel uses the radius of the sphere of equal
+                volume r0 = (3 dV / 4 pi)^(1/3).  Normalised (on the GPU, FP64) so the
+                kernel sums to 1, then scaled to Gy/(Bq s) by the mean beta energy.
+  "reference" : restatement of the reference generators
+                (data/dose_kernels/y90_kernel.py:20-140, lu177_kernel.py:52-184) with the
+                r = 0 singularity of the photon term replaced by r0 (the reference
+                produces NaN there, y90_kernel.py:134-138).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+JOULE_PER_MEV = 1.602176634e-13
+
+
+@dataclass(frozen=True)
+class Nuclide:
+    symbol: str
+    half_life_h: float
+    beta_mean_mev: float
+    beta_max_mev: float
+    beta_csda_range_mm: float
+    kernel_reach_mm: float                     # half-width of the default kernel grid
+    spectrum_e: tuple = ()                     # beta spectrum sample energies (MeV)
+    spectrum_p: tuple = ()                     # relative probability density at spectrum_e
+    gammas: tuple = ()                         # ((energy MeV, photons per decay), ...)
+    beta_branches: tuple = ()                  # ((Emax MeV, abundance), ...) for the reference generator
+    extra: dict = field(default_factory=dict)
+
+
+NUCLIDES = {
+    "Y90": Nuclide("Y90", 64.1, 0.934, 2.280, 11.3, 15.0,
+                   spectrum_e=(0.0, 0.2, 0.4, 0.6, 0.8, 1.0, 1.2, 1.4, 1.6, 1.8, 2.0, 2.2, 2.280),
+                   spectrum_p=(0.0, 0.12, 0.22, 0.30, 0.36, 0.40, 0.42, 0.38, 0.32, 0.24, 0.15, 0.06, 0.0),
+                   beta_branches=((2.280, 1.0),)),
+    "Lu177": Nuclide("Lu177", 6.647 * 24.0, 0.149, 0.498, 1.7, 6.0,
+                     spectrum_e=(0.0, 0.1, 0.2, 0.3, 0.4, 0.498),
+                     spectrum_p=(0.0, 0.35, 0.48, 0.42, 0.22, 0.0),
+                     gammas=((0.208, 0.1094), (0.113, 0.0641)),
+                     beta_branches=((0.498, 0.795), (0.385, 0.089), (0.177, 0.116))),
+    "I131": Nuclide("I131", 8.0207 * 24.0, 0.182, 0.807, 3.2, 7.5,
+                    spectrum_e=(0.0, 0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.807),
+                    spectrum_p=(0.0, 0.25, 0.42, 0.48, 0.42, 0.32, 0.20, 0.08, 0.0),
+                    gammas=((0.364, 0.812), (0.637, 0.0717), (0.284, 0.0606))),
+    "F18": Nuclide("F18", 1.8295, 0.250, 0.634, 2.4, 6.0),
+    "Ga68": Nuclide("Ga68", 1.128, 0.836, 1.899, 9.0, 12.0),
+    "Tb161": Nuclide("Tb161", 165.432, 0.154, 0.593, 1.8, 6.0),
+}
+
+# Tissue properties used by the reference generators (y90_kernel.py:57-91, lu177_kernel.py:88-127).
+TISSUES = {
+    "water": dict(density=1.0, effective_Z=7.42, stopping_power_ratio=1.0, mu_by_rho=0.096, scale=1.0),
+    "lung": dict(density=0.26, effective_Z=7.41, stopping_power_ratio=1.04, mu_by_rho=0.095, scale=1.04),
+    "soft_tissue": dict(density=1.04, effective_Z=7.46, stopping_power_ratio=1.04, mu_by_rho=0.097, scale=1.04),
+    "bone": dict(density=1.85, effective_Z=13.8, stopping_power_ratio=1.15, mu_by_rho=0.110, scale=1.15),
+    "iodine_contrast": dict(density=1.30, effective_Z=53.0, stopping_power_ratio=1.12, mu_by_rho=0.245, scale=1.12),
+}
+
+Y90_LAMBDA_MM = 1.8
+
+
+def get_nuclide(symbol: str) -> Nuclide:
+    try:
+        return NUCLIDES[symbol]
+    except KeyError:
+        raise ValueError(f"Unsupported nuclide: {symbol}. Supported: {sorted(NUCLIDES)}") from None
+
+
+def _vox3(voxel_size):
+    if np.isscalar(voxel_size):
+        return (float(voxel_size),) * 3
+    v = tuple(float(x) for x in voxel_size)
+    if len(v) != 3:
+        raise ValueError("voxel_size must be a scalar or a 3-tuple")
+    return v
+
+
+def default_kernel_size(symbol: str, voxel_size) -> tuple:
+    """Odd kernel dims covering +/- the nuclide's kernel reach (15 mm Y-90, 6 mm Lu-177,
+    7.5 mm I-131): 15^3 at 2 mm and 21^3 at 1.5 mm for Y-90, 9^3 / 11^3 at 1.5 mm."""
+    nuc = get_nuclide(symbol)
+    return tuple(2 * int(math.floor(nuc.kernel_reach_mm / d + 1e-9)) + 1 for d in _vox3(voxel_size))
+
+
+def radius_grid(shape, voxel_size) -> np.ndarray:
+    """Distance (mm) of each kernel voxel centre from the centre voxel shape//2."""
+    v = _vox3(voxel_size)
+    idx = np.indices(shape, dtype=np.float64)
+    return np.sqrt(sum(((idx[i] - shape[i] // 2) * v[i]) ** 2 for i in range(3)))
+
+
+def equal_volume_radius(voxel_size) -> float:
+    v = _vox3(voxel_size)
+    return (3.0 * v[0] * v[1] * v[2] / (4.0 * math.pi)) ** (1.0 / 3.0)
+
+
+def analytic_lambda_mm(symbol: str) -> float:
+    nuc = get_nuclide(symbol)
+    return Y90_LAMBDA_MM * nuc.beta_csda_range_mm / NUCLIDES["Y90"].beta_csda_range_mm
+
+
+def analytic_profile(symbol: str, voxel_size, shape=None) -> np.ndarray:
+    """Un-normalised exp(-r/lambda)/r^2 kernel (FP64), centre voxel at r0."""
+    shape = tuple(shape) if shape is not None else default_kernel_size(symbol, voxel_size)
+    r = radius_grid(shape, voxel_size)
+    r = np.where(r == 0.0, equal_volume_radius(voxel_size), r)
+    lam = analytic_lambda_mm(symbol)
+    return np.exp(-r / lam) / (r * r)
+
+
+def gy_per_bq_s_scale(symbol: str, voxel_size, water_density: float = 1.0) -> float:
+    """Mean beta energy per decay deposited in one voxel of water, in Gy per (Bq s):
+    E_mean [MeV] * 1.602176634e-13 [J/MeV] / (rho * dV [mm^3] * 1e-6 [kg / (g/cc mm^3)])."""
+    v = _vox3(voxel_size)
+    return get_nuclide(symbol).beta_mean_mev * JOULE_PER_MEV / (water_density * v[0] * v[1] * v[2] * 1e-6)
+
+
+# --------------------------------------------------------------------------
+# restatement of the reference generators
+# --------------------------------------------------------------------------
+def _beta_cole(r, e_max, coef, tissue):
+    """(1 - r/R)^2 exp(-2 r/R) * rho * SPR for r <= R, R = coef * Emax^1.5 / rho / SPR
+    (y90_kernel.py:93-117 with coef 11; lu177_kernel.py:129-154 with coef 5)."""
+    rho, spr = tissue["density"], tissue["stopping_power_ratio"]
+    rng = coef * e_max ** 1.5 * (1.0 / rho) * (1.0 / spr)
+    out = np.zeros_like(r)
+    m = r <= rng
+    out[m] = (1 - r[m] / rng) ** 2 * np.exp(-2 * r[m] / rng) * rho * spr
+    return out
+
+
+def reference_profile(symbol: str, tissue: str, voxel_size: float, shape, fix_r0: bool = True) -> np.ndarray:
+    """The reference's Y-90 / Lu-177 generator kernels (isotropic voxel).
+
+    Y-90: Cole beta term + bremsstrahlung 0.015 (Z/7.42)^2 rho exp(-mu r/10)/(4 pi r^2),
+    mu = 0.096 rho /cm, times the tissue scaling factor (y90_kernel.py:20-55, 119-161).
+    Lu-177: abundance-weighted Cole terms (5 Emax^1.5 range) + gamma lines
+    I exp(-mu r/10)/(4 pi r^2), mu = rho (mu/rho) (0.2/E)^3.2 (lu177_kernel.py:52-86, 156-184).
+    With ``fix_r0`` the photon terms use r0 at the centre voxel instead of the
+    reference's 0 * inf = NaN.
+    """
+    t = TISSUES.get(tissue, TISSUES["water"])
+    r = radius_grid(tuple(shape), voxel_size)
+    rc = np.where(r == 0.0, equal_volume_radius(voxel_size), r) if fix_r0 else r
+    nuc = get_nuclide(symbol)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        if symbol == "Y90":
+            k = _beta_cole(r, nuc.beta_max_mev, 11.0, t)
+            mu = 0.096 * (t["density"] / 1.0)
+            rel_yield = (t["effective_Z"] / 7.42) ** 2
+            brems = 0.015 * rel_yield * t["density"] * np.exp(-mu * rc / 10) / (4 * np.pi * rc ** 2)
+            if not fix_r0:
+                brems = brems * (r > 0)
+            k = k + brems
+            k = k * t["scale"]
+        elif symbol == "Lu177":
+            k = np.zeros_like(r)
+            for e_max, ab in nuc.beta_branches:
+                k += ab * _beta_cole(r, e_max, 5.0, t)
+            for e_g, inten in ((0.208, 0.111), (0.113, 0.062)):  # dose_kernels/Lu177/Lu177.json:23-26
+                mu = t["density"] * t["mu_by_rho"] * (0.2 / e_g) ** 3.2
+                g = inten * np.exp(-mu * rc / 10) / (4 * np.pi * rc ** 2)
+                if not fix_r0:
+                    g = np.where(r > 0, g, 0.0)
+                k += g
+        else:
+            raise ValueError(f"no reference generator for {symbol} (the reference ships Y90 and Lu177 only)")
+    return k

@@ -1,0 +1,64 @@
+"""The oracle against vectors recorded from the reference implementation itself
+(tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+from oracle import conv as oc
+from oracle import time_fit as of
+
+
+@pytest.mark.parametrize("name", ["ragged_asym", "cube_radial", "oversize", "even_kernel", "thin"])
+def test_circular_conv_is_reference(golden, name):
+    d = oc.reference_circular_conv(golden[f"conv_{name}_A"], golden[f"conv_{name}_K"])
+    np.testing.assert_allclose(d, golden[f"conv_{name}_D"], rtol=0, atol=1e-12 * np.abs(d).max())
+
+
+def test_trapezoid_is_reference(golden):
+    out = oc.trapezoid_activity(list(golden["trap_maps"]), list(golden["trap_times"]))
+    np.testing.assert_allclose(out, golden["trap_out"], rtol=1e-14)
+
+
+def test_trapezoid_weights_reproduce_trapezoid(golden):
+    w = oc.trapezoid_weights(golden["trap_times"])
+    out = np.tensordot(w, golden["trap_maps"], axes=1)
+    np.testing.assert_allclose(out, golden["trap_out"], rtol=1e-12)
+
+
+def test_absorbed_dose_is_reference(golden):
+    rates = [oc.reference_circular_conv(m, golden["absd_K"]) for m in golden["absd_maps"]]
+    out = oc.absorbed_dose_from_rates(rates, list(golden["absd_times"]))
+    np.testing.assert_allclose(out, golden["absd_out"], rtol=1e-12)
+
+
+def test_linear_conv_equals_direct_sum():
+    rng = np.random.default_rng(3)
+    a = rng.random((6, 5, 7))
+    k = rng.random((3, 5, 3))
+    d = oc.linear_conv_same(a, k)
+    c = [s // 2 for s in k.shape]
+    ref = np.zeros_like(a)
+    for i in np.ndindex(a.shape):
+        s = 0.0
+        for j in np.ndindex(k.shape):
+            src = tuple(i[t] - j[t] + c[t] for t in range(3))
+            if all(0 <= src[t] < a.shape[t] for t in range(3)):
+                s += a[src] * k[j]
+        ref[i] = s
+    np.testing.assert_allclose(d, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_mono_fit_is_reference(golden):
+    p, auc = of.fit_mono(golden["fit_times"], list(golden["fit_acts"]), 64.1)
+    np.testing.assert_allclose(p, golden["fit_params"], rtol=1e-12, atol=0)
+    np.testing.assert_array_equal(np.isnan(auc), np.isnan(golden["fit_auc"]))
+    np.testing.assert_allclose(auc, golden["fit_auc"], rtol=1e-12)
+    p, auc = of.fit_mono(golden["fit_times"], list(golden["fit_acts"]), 64.1, weight_factors=list(golden["fit_w"]))
+    np.testing.assert_allclose(p, golden["fit_params_w"], rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("model,name", [("nukfit", "f2"), ("lmfit", "mono-exponential")])
+def test_advanced_fit_is_reference(golden, model, name):
+    p, auc, ok = of.fit_advanced(golden["adv_times"], list(golden["adv_acts"]), 64.1, model=model, model_name=name)
+    key = name.replace("-", "_")
+    np.testing.assert_allclose(p, golden[f"adv_{key}_params"], rtol=1e-12)
+    np.testing.assert_allclose(auc, golden[f"adv_{key}_auc"], rtol=1e-12)
