@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Dose-convolution throughput on GB300 (one JSON line on rank 0).
+
+Workload (default ``ct256_y90_lu177_i131``): a seeded 256^3 CT-like phantom at
+1.5 mm (density + activity), dose-point-kernel convolution with three nuclide
+kernels (Y-90 21^3, Lu-177 9^3, I-131 11^3, analytic radial profiles) sharing
+one forward transform, density-scaled epilogue.  One step = the three dose
+maps of one volume; the metric counts output dose voxels (3 x 256^3 per step).
+``sphere128_y90`` is the 128^3 / 2 mm / 15^3 single-kernel water case.
+
+value : device-resident inputs, CUDA events on the launching stream around
+        each step, L2 flushed (256 MiB write) between steps outside the events.
+e2e   : the same workload through the public API
+        (KernelConvolutionCalculator.calculate_dose_rate) from pinned host
+        tensors: H2D of activity+density and D2H of the dose maps inside the
+        timed region.
+roofline : the dominant pass, timed live with CUDA events (pvd_plan_profile)
+        over the timed steps; algorithmic bytes from the pass byte model.
+cpu_baseline : the reference operator (numpy FFT, float64, single thread)
+        on one full-size Y-90 convolution, timed on this host.
+``--impl reference`` times that CPU path alone as the reference arm.
+
+Multi-GPU (torchrun): independent replicas, one volume per rank per step
+(weak scaling); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+METRIC = "dose Gvoxel/s: plain conv vs NN-corrected (≤3% vs MC), % of HBM roofline"
+UNIT = "Gvoxel/s"
+
+WORKLOADS = {
+    "ct256_y90_lu177_i131": dict(shape=(256, 256, 256), voxel_mm=1.5, phantom="ct",
+                                 nuclides=["Y90", "Lu177", "I131"], ksize={"Y90": 21, "Lu177": 9, "I131": 11},
+                                 density=True),
+    "sphere128_y90": dict(shape=(128, 128, 128), voxel_mm=2.0, phantom="sphere", nuclides=["Y90"],
+                          ksize={"Y90": 15}, density=False),
+}
+PASS_NAMES = ["x_fwd", "y_fwd", "z_fwd_mul_inv", "y_inv", "x_inv"]
+PASS_KERNELS = ["k_x_fwd", "k_y<false>", "k_z", "k_y<true>", "k_x_inv"]
+
+
+def make_inputs(wl):
+    from pyvoxeldosimetry_gb300 import phantoms
+    if wl["phantom"] == "ct":
+        act, rho = phantoms.ct_phantom(wl["shape"], wl["voxel_mm"], seed=2)
+    else:
+        act = phantoms.sphere_phantom(wl["shape"], wl["voxel_mm"], seed=1)
+        rho = None
+    return act, (rho if wl["density"] else None)
+
+
+def byte_model(shape, kmax, nk, density):
+    """Algorithmic HBM bytes per pass launch of the pruned 5-pass R2C pipeline at the
+    minimal padding P = N + K - 1 (padding beyond that is the implementation's cost).
+    x_fwd: 4V + A; y_fwd: A + By; z: per kernel By + S + By (multi-kernel launch counts
+    every kernel); y_inv: By + A; x_inv: A + 4V (+4V density)."""
+    n0, n1, n2 = shape
+    p = [n + k - 1 for n, k in zip(shape, kmax)]
+    h = p[2] // 2 + 1
+    v = n0 * n1 * n2
+    a = 8 * n0 * n1 * h
+    by = 8 * p[1] * n0 * h
+    s = 4 * p[0] * p[1] * h
+    return {
+        "x_fwd": 4 * v + a,
+        "y_fwd": a + by,
+        "z_fwd_mul_inv": nk * (2 * by + s),
+        "y_inv": by + a,
+        "x_inv": a + 4 * v + (4 * v if density else 0),
+        "_per_step": (4 * v + a) + (a + by) + nk * (2 * by + s) + nk * (by + a) + nk * (a + 4 * v + (4 * v if density else 0)),
+        "_compulsory_per_step": 4 * v * (1 + (1 if density else 0) + nk) + nk * s,
+        "_p_min": p,
+    }
+
+
+def load_peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "fallback (6.8 TB/s)"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms during the timed region."""
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self.gpu_id, f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_reference_conv(act, rho, kernel):
+    """The reference operator (core/kernel_convolution.py:71-74) in float64 on zero-padded
+    inputs, cropped, density-divided: the CPU path a reference user runs."""
+    from oracle import conv as oc
+    d = oc.linear_conv_same(act.astype(np.float64), kernel)
+    return oc.density_scale(d, rho)
+
+
+def reference_kernels(wl):
+    from pyvoxeldosimetry_gb300.data import nuclides as nd
+    out = []
+    for nuc in wl["nuclides"]:
+        k = nd.analytic_profile(nuc, wl["voxel_mm"], (wl["ksize"][nuc],) * 3)
+        out.append(k / k.sum() * nd.gy_per_bq_s_scale(nuc, wl["voxel_mm"]))
+    return out
+
+
+def run_reference(args, wl, rank):
+    """Reference arm: the reference's CPU convolution operator on this host, one
+    full-size nuclide convolution per step (nuclides in turn)."""
+    if rank != 0:
+        return
+    act, rho = make_inputs(wl)
+    ks = reference_kernels(wl)
+    vox = int(np.prod(wl["shape"]))
+    for i in range(args.warmup):
+        cpu_reference_conv(act, rho, ks[i % len(ks)])
+    times = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        cpu_reference_conv(act, rho, ks[i % len(ks)])
+        times.append(time.perf_counter() - t0)
+    t = float(np.sum(times))
+    value = vox * args.steps / t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded phantom)",
+        "config": config_dict(args.workload, wl),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"one full {wl['shape']} convolution per step (nuclides in turn), numpy "
+                                   "float64 FFT of the reference operator on zero-padded inputs + density divide"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(name, wl):
+    return {"workload": name, "shape": list(wl["shape"]), "voxel_mm": wl["voxel_mm"],
+            "kernels": {n: [wl["ksize"][n]] * 3 for n in wl["nuclides"]}, "density_scaled": wl["density"],
+            "voxels_per_step": int(np.prod(wl["shape"])) * len(wl["nuclides"]),
+            "l2": "flushed between timed steps (256 MiB write, outside the events)",
+            "parallelism": "replicas (one volume per GPU)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ct256_y90_lu177_i131", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    wl = WORKLOADS[args.workload]
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, wl, rank)
+        return
+
+    import torch
+    import torch.distributed as dist
+
+    torch.cuda.set_device(local_rank)
+    device = torch.device("cuda", local_rank)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=device)
+
+    from pyvoxeldosimetry_gb300 import _native as N
+    from pyvoxeldosimetry_gb300.core.kernel_convolution import KernelConvolutionCalculator
+
+    lib = N.load()
+    act, rho = make_inputs(wl)
+    shape = wl["shape"]
+    vox = int(np.prod(shape))
+    nk = len(wl["nuclides"])
+    vs = (wl["voxel_mm"],) * 3
+    calc = KernelConvolutionCalculator(wl["nuclides"], config={"kernel_size": wl["ksize"], "device": device})
+    plan = calc._plan_for(shape, vs, device)
+    act_d = torch.from_numpy(act).to(device)
+    rho_d = torch.from_numpy(rho).to(device) if rho is not None else None
+    out_d = torch.empty((nk, *shape), dtype=torch.float32, device=device)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=device)  # 256 MiB > 129 MB L2
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for i in range(args.warmup):
+        flush.fill_(float(i))
+        plan.execute(act_d, density=rho_d, out=out_d)
+    torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    N.check(lib.pvd_plan_profile(plan._h, 1))
+    lib.pvd_launch_count(1)
+    gpu_id = str(local_rank)
+    try:
+        uuid = str(torch.cuda.get_device_properties(device).uuid)
+        gpu_id = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+    except Exception:
+        pass
+    with ClockSampler(gpu_id) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.fill_(float(i))
+            evs[i][0].record(stream)
+            plan.execute(act_d, density=rho_d, out=out_d)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    launches = int(lib.pvd_launch_count(0))
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = float(np.sum(step_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_arr = (ctypes.c_double * 5)()
+    cnt_arr = (ctypes.c_int * 5)()
+    N.check(lib.pvd_plan_pass_times(plan._h, ms_arr, cnt_arr))
+    N.check(lib.pvd_plan_profile(plan._h, 0))
+    pass_ms = {PASS_NAMES[i]: float(ms_arr[i]) for i in range(5)}
+    pass_n = {PASS_NAMES[i]: int(cnt_arr[i]) for i in range(5)}
+    value = world * nk * vox * args.steps / (total_ms / 1e3) / 1e9
+
+    # roofline of the dominant pass
+    kmax = [max(wl["ksize"][n] for n in wl["nuclides"])] * 3
+    bm = byte_model(shape, kmax, nk, wl["density"])
+    peak, peak_src = load_peaks()
+    dom = max(PASS_NAMES, key=lambda k: pass_ms[k])
+    avg_s = pass_ms[dom] / max(pass_n[dom], 1) / 1e3
+    achieved = bm[dom] / avg_s / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(args.workload, {}).get(PASS_KERNELS[PASS_NAMES.index(dom)])
+    step_s = total_ms / args.steps / 1e3
+    roofline = {"bound": "hbm", "kernel": PASS_KERNELS[PASS_NAMES.index(dom)], "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                "algorithmic_bytes_per_launch": bm[dom], "peak_source": peak_src,
+                "pass_ms_per_step": {k: pass_ms[k] / args.steps for k in PASS_NAMES},
+                "pipeline_achieved": bm["_per_step"] / step_s / 1e9,
+                "pipeline_frac": bm["_per_step"] / step_s / 1e9 / peak,
+                "compulsory_frac": bm["_compulsory_per_step"] / step_s / 1e9 / peak,
+                "fft_shape": list(plan.fft_shape), "p_min": bm["_p_min"]}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom)",
+            "config": config_dict(args.workload, wl), "roofline": roofline, "gpu_launches": launches,
+            "clocks": clk.summary()}
+
+    # end to end through the public API from pinned host memory
+    if not args.no_e2e:
+        act_h = torch.from_numpy(act).pin_memory()
+        rho_h = torch.from_numpy(rho).pin_memory() if rho is not None else None
+        out_h = torch.empty((nk, *shape), dtype=torch.float32, pin_memory=True)
+        for i in range(args.warmup):
+            calc.calculate_dose_rate(act_h, vs, density=rho_h, out=out_h)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        barrier()
+        torch.cuda.synchronize()
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            calc.calculate_dose_rate(act_h, vs, density=rho_h, out=out_h)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        barrier()
+        e2e_ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
+        if world > 1:
+            t = torch.tensor([e2e_ms], device=device)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        line["e2e"] = {"value": world * nk * vox * args.steps / (e2e_ms / 1e3) / 1e9, "unit": UNIT,
+                       "h2d_bytes_per_step": 4 * vox * (2 if rho is not None else 1),
+                       "d2h_bytes_per_step": 4 * vox * nk, "ms_per_step": e2e_ms / args.steps,
+                       "wall_ms_per_step": 1e3 * wall / args.steps,
+                       "api": "KernelConvolutionCalculator.calculate_dose_rate(pinned CPU tensors)"}
+
+    if rank == 0 and not args.no_cpu_baseline:
+        ks = reference_kernels(wl)
+        t0 = time.perf_counter()
+        cpu_reference_conv(act, rho, ks[0])
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": vox / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"one full {list(shape)} {wl['nuclides'][0]} convolution: numpy float64 "
+                                          "FFT of the reference operator on zero-padded inputs + density divide",
+                                "seconds": dt}
+    if world > 1:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

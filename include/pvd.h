@@ -130,6 +130,51 @@ pvd_status pvd_conv_execute_weighted(pvd_plan* plan, const float* const* activit
 
 pvd_status pvd_plan_destroy(pvd_plan* plan);
 
+/* Per-pass timing (instrumentation; not part of the reference interface).
+ * pvd_plan_profile(plan, 1) resets the records and brackets every later pass
+ * launch of this plan with CUDA events on its stream; pvd_plan_pass_times
+ * waits for the recorded events and returns, per pass kind, the summed
+ * milliseconds and the number of launches:
+ *   0 x-forward (R2C), 1 y-forward, 2 z (forward * spectrum * inverse),
+ *   3 y-inverse, 4 x-inverse (C2R, crop, scale, density). */
+#define PVD_NUM_PASSES 5
+pvd_status pvd_plan_profile(pvd_plan* plan, int enable);
+pvd_status pvd_plan_pass_times(pvd_plan* plan, double* ms, int* launches);
+
+/* ------------------------------------------------------------------------ */
+/* Time integration                                                           */
+/* ------------------------------------------------------------------------ */
+
+/* out[i] = sum_t weights[t] * maps[t][i] over n_voxels float32 voxels (device
+ * pointers, t < n_maps <= PVD_MAX_TIMEPOINTS).  With trapezoid weights this is
+ * ActivitySampler._trapezoid_integration (core/activity_sampler.py:69-78). */
+pvd_status pvd_weighted_sum(const float* const* maps, const float* weights, int n_maps,
+                            long long n_voxels, float* out, pvd_stream stream);
+
+/* Per-voxel time-activity-curve fit (FP64, one thread per voxel).
+ * Models (the reference's curve_fitting.py):
+ *   PVD_FIT_MONO_LAMBDA  A0 exp(-lam t), p = [A0, lam]; p0 = [y(t0), lam_phys]
+ *                        unless PVD_FIT_P0_GIVEN; failure -> [0, lam_phys];
+ *                        auc = A0/lam (1 - exp(-lam auc_limit))      (:19-84)
+ *   PVD_FIT_F2..F4C      NUKFIT f2, f3, f3a, f4a, f4b, f4c (lam_phys added to
+ *                        every rate), PVD_FIT_LM_MONO/BI/TRI the "lmfit" table;
+ *                        p0 required; failure -> zeros; auc = trapezoid of the
+ *                        fitted curve over the sampled times              (:112-219)
+ * Residuals are weights[k] * (f(t_k) - y_k) (curve_fit with sigma = 1/weights;
+ * weights may be NULL = 1).  acts_d: device float32 [n_times][n_vox];
+ * params_d: device float64 [n_par][n_vox]; auc_d: device float64 [n_vox];
+ * ok_d: device uint8 [n_vox] (1 = converged) or NULL.  max_iter bounds the
+ * Levenberg-Marquardt iterations (non-convergence is a failure). */
+enum {
+  PVD_FIT_MONO_LAMBDA = 0, PVD_FIT_F2 = 1, PVD_FIT_F3 = 2, PVD_FIT_F3A = 3, PVD_FIT_F4A = 4,
+  PVD_FIT_F4B = 5, PVD_FIT_F4C = 6, PVD_FIT_LM_MONO = 7, PVD_FIT_LM_BI = 8, PVD_FIT_LM_TRI = 9
+};
+enum { PVD_FIT_FORCE_ZERO_AT_T0 = 1, PVD_FIT_P0_GIVEN = 2 };
+pvd_status pvd_tac_fit(int model, const double* times, const double* weights, int n_times,
+                       const double* p0, double lam_phys, double auc_limit, int max_iter, int flags,
+                       const float* acts_d, long long n_vox, double* params_d, double* auc_d,
+                       unsigned char* ok_d, pvd_stream stream);
+
 /* ------------------------------------------------------------------------ */
 /* Misc                                                                       */
 /* ------------------------------------------------------------------------ */

@@ -1,0 +1,22 @@
+"""GB300-native (sm_103a) voxel dosimetry: a drop-in for the dose-calculation
+hot path of devhliu/PyVoxelDosimetry.
+
+Public names mirror the reference package (pyvoxeldosimetry/__init__.py:8-21,
+pyvoxeldosimetry/core/__init__.py:7-24).  All dose arithmetic runs in the CUDA
+library ``libpvd_gb300.so`` behind the C ABI in ``include/pvd.h``; importing
+this package does not need a GPU, using it does.
+"""
+__version__ = "0.1.0"
+
+from .core.dosimetry_base import DosimetryCalculator
+from .core.kernel_convolution import KernelConvolutionCalculator
+from .core.activity_sampler import ActivitySampler
+from .core.dose_calculator import DoseCalculator, DoseCalculationResult
+
+__all__ = [
+    "DosimetryCalculator",
+    "KernelConvolutionCalculator",
+    "ActivitySampler",
+    "DoseCalculator",
+    "DoseCalculationResult",
+]

@@ -445,6 +445,12 @@ struct pvd_plan {
   size_t ws_bytes = 0;
   size_t smem_x = 0, smem_y = 0, smem_z = 0;
   std::vector<void*> allocs;
+  // per-pass event timing (instrumentation, off by default)
+  int prof = 0;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  struct Rec { int kind; cudaEvent_t a, b; };
+  std::vector<Rec> recs;
 };
 
 namespace {
@@ -465,7 +471,36 @@ pvd_status plan_alloc(pvd_plan* p, size_t bytes, void** out) {
 void plan_free(pvd_plan* p) {
   for (void* a : p->allocs) cudaFree(a);
   p->allocs.clear();
+  for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+  p->ev_pool.clear();
 }
+
+cudaEvent_t prof_event(pvd_plan* p) {
+  if (p->ev_used == p->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    p->ev_pool.push_back(e);
+  }
+  return p->ev_pool[p->ev_used++];
+}
+
+// Brackets one pass launch with events on `st` when profiling is enabled.
+struct PassTimer {
+  pvd_plan* p;
+  int kind;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr;
+  PassTimer(pvd_plan* p_, int kind_, cudaStream_t st_) : p(p_), kind(kind_), st(st_) {
+    if (p->prof && (a = prof_event(p))) cudaEventRecord(a, st);
+  }
+  ~PassTimer() {
+    if (!a) return;
+    cudaEvent_t b = prof_event(p);
+    if (!b) return;
+    cudaEventRecord(b, st);
+    p->recs.push_back({kind, a, b});
+  }
+};
 
 size_t smem_bytes(int L, int nbuf) { return (size_t)(L + nbuf * L * TXP) * sizeof(float2); }
 
@@ -684,10 +719,16 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
   const int xblocks = (nrows + 2 * TX - 1) / (2 * TX);
   const int ctiles = p->HS / TX;
 
-  k_x_fwd<<<xblocks, NT, p->smem_x, st>>>(in, p->buf1, nrows, N2, p->HS, p->f[2], p->tw[2]);
-  PVD_LAUNCH_CHECK("k_x_fwd");
-  k_y<false><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf1, p->buf2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
-  PVD_LAUNCH_CHECK("k_y<fwd>");
+  {
+    PassTimer t(p, 0, st);
+    k_x_fwd<<<xblocks, NT, p->smem_x, st>>>(in, p->buf1, nrows, N2, p->HS, p->f[2], p->tw[2]);
+    PVD_LAUNCH_CHECK("k_x_fwd");
+  }
+  {
+    PassTimer t(p, 1, st);
+    k_y<false><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf1, p->buf2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
+    PVD_LAUNCH_CHECK("k_y<fwd>");
+  }
   OutSet os;
   std::memset(&os, 0, sizeof(os));
   os.n = p->nk;
@@ -696,14 +737,23 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
     os.s[s] = p->spec[s];
     os.real[s] = p->spec_real[s];
   }
-  k_z<<<dim3(ctiles, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
-  PVD_LAUNCH_CHECK("k_z");
+  {
+    PassTimer t(p, 2, st);
+    k_z<<<dim3(ctiles, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
+    PVD_LAUNCH_CHECK("k_z");
+  }
   for (int s = 0; s < p->nk; ++s) {
-    k_y<true><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS, p->f[1], p->tw[1]);
-    PVD_LAUNCH_CHECK("k_y<inv>");
-    k_x_inv<<<xblocks, NT, p->smem_x, st>>>(p->buf1, dose + s * vox, rho, nrows, N2, p->HS, out_scale, p->f[2],
-                                           p->tw[2]);
-    PVD_LAUNCH_CHECK("k_x_inv");
+    {
+      PassTimer t(p, 3, st);
+      k_y<true><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS, p->f[1], p->tw[1]);
+      PVD_LAUNCH_CHECK("k_y<inv>");
+    }
+    {
+      PassTimer t(p, 4, st);
+      k_x_inv<<<xblocks, NT, p->smem_x, st>>>(p->buf1, dose + s * vox, rho, nrows, N2, p->HS, out_scale, p->f[2],
+                                             p->tw[2]);
+      PVD_LAUNCH_CHECK("k_x_inv");
+    }
   }
   return PVD_OK;
 }
@@ -734,6 +784,32 @@ extern "C" pvd_status pvd_conv_execute_weighted(pvd_plan* p, const float* const*
     in.w[t] = w[t];
   }
   return conv_run(p, in, rho, dose, out_scale, stream);
+}
+
+extern "C" pvd_status pvd_plan_profile(pvd_plan* p, int enable) {
+  if (!p) return set_error(PVD_ERR_ARG, "pvd_plan_profile: null plan");
+  p->prof = enable ? 1 : 0;
+  p->recs.clear();
+  p->ev_used = 0;
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_plan_pass_times(pvd_plan* p, double* ms, int* launches) {
+  if (!p || !ms || !launches) return set_error(PVD_ERR_ARG, "pvd_plan_pass_times: null argument");
+  for (int i = 0; i < PVD_NUM_PASSES; ++i) {
+    ms[i] = 0.0;
+    launches[i] = 0;
+  }
+  for (const auto& r : p->recs) {
+    cudaError_t e = cudaEventSynchronize(r.b);
+    if (e != cudaSuccess) return cuda_error(e, "pvd_plan_pass_times");
+    float t = 0.f;
+    e = cudaEventElapsedTime(&t, r.a, r.b);
+    if (e != cudaSuccess) return cuda_error(e, "pvd_plan_pass_times");
+    ms[r.kind] += t;
+    launches[r.kind] += 1;
+  }
+  return PVD_OK;
 }
 
 extern "C" pvd_status pvd_plan_destroy(pvd_plan* p) {
