@@ -130,6 +130,11 @@ pvd_status pvd_conv_execute_weighted(pvd_plan* plan, const float* const* activit
 
 pvd_status pvd_plan_destroy(pvd_plan* plan);
 
+/* FFT lengths that have register-resident (four-step) pass kernels; LINEAR
+ * plans pad to one of them when it costs <= 25 % over the minimum.  Writes up
+ * to `cap` lengths (ascending) and returns how many exist. */
+int pvd_fast_lengths(int* out, int cap);
+
 /* Per-pass timing (instrumentation; not part of the reference interface).
  * pvd_plan_profile(plan, 1) resets the records and brackets every later pass
  * launch of this plan with CUDA events on its stream; pvd_plan_pass_times

@@ -29,6 +29,8 @@
 #include <string>
 #include <vector>
 
+#include "conv_types.cuh"
+#include "fft_fast.cuh"
 #include "pvd_common.cuh"
 
 namespace pvd {
@@ -43,19 +45,6 @@ struct FftLen {
   int L;
   int nst;
   int rad[MAX_STAGES];
-};
-
-struct ActIn {
-  const float* p[PVD_MAX_TIMEPOINTS];
-  float w[PVD_MAX_TIMEPOINTS];
-  int n;
-};
-
-struct OutSet {
-  float2* p[PVD_MAX_KERNELS];
-  const void* s[PVD_MAX_KERNELS];
-  int real[PVD_MAX_KERNELS];
-  int n;
 };
 
 // ---------------------------------------------------------------------------
@@ -259,18 +248,19 @@ __global__ void __launch_bounds__(NT) k_z(const float2* __restrict__ in, OutSet 
       A = bufs[1 - xi];
       B = bufs[2];
     }
-    const long long sbase = (long long)ky * HS + kx0;
-    if (os.real[s]) {
+    if (os.mode[s] == SPEC_REAL_EVEN) {
       const float* S = (const float*)os.s[s];
+      const int kyq = min(ky, P1 - ky);
       for (int idx = threadIdx.x; idx < TX * f.L; idx += NT) {
         const int z = idx / TX, c = idx % TX;
-        A[z * TXP + c] = cscale(X[z * TXP + c], __ldg(S + z * zstride + sbase + c));
+        const int kzq = min(z, os.P0 - z);
+        A[z * TXP + c] = cscale(X[z * TXP + c], __ldg(S + ((long long)kzq * os.P1h + kyq) * HS + kx0 + c));
       }
     } else {
       const float2* S = (const float2*)os.s[s];
       for (int idx = threadIdx.x; idx < TX * f.L; idx += NT) {
         const int z = idx / TX, c = idx % TX;
-        A[z * TXP + c] = cmul(X[z * TXP + c], __ldg(S + z * zstride + sbase + c));
+        A[z * TXP + c] = cmul(X[z * TXP + c], __ldg(S + z * zstride + (long long)ky * HS + kx0 + c));
       }
     }
     __syncthreads();
@@ -397,14 +387,17 @@ __global__ void k_spec_y(const float2* __restrict__ t1, float2* __restrict__ t2,
   }
 }
 
-// S[kz][ky][kx] = sum_m0 T2[m0][ky][kx] w0^(kz * ((m0 - o0) mod P0)); kx in [H, HS) -> 0
-__global__ void k_spec_z(const float2* __restrict__ t2, void* __restrict__ spec, int real_out, int K0e, int o0,
-                         int P0, int P1, int H, int HS, const float2* __restrict__ tw0) {
-  const long long total = (long long)P0 * P1 * HS;
+// S[kz][ky][kx] = sum_m0 T2[m0][ky][kx] w0^(kz * ((m0 - o0) mod P0)); kx in [H, HS) -> 0.
+// SPEC_REAL_EVEN stores the real part for kz <= P0/2, ky <= P1/2 only.
+__global__ void k_spec_z(const float2* __restrict__ t2, void* __restrict__ spec, int mode, int K0e, int o0, int P0,
+                         int P1, int H, int HS, const float2* __restrict__ tw0) {
+  const int nz = (mode == SPEC_REAL_EVEN) ? P0 / 2 + 1 : P0;
+  const int ny = (mode == SPEC_REAL_EVEN) ? P1 / 2 + 1 : P1;
+  const long long total = (long long)nz * ny * HS;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
     const int kx = (int)(i % HS);
-    const int ky = (int)((i / HS) % P1);
-    const int kz = (int)(i / ((long long)HS * P1));
+    const int ky = (int)((i / HS) % ny);
+    const int kz = (int)(i / ((long long)HS * ny));
     float2 acc = make_float2(0.f, 0.f);
     if (kx < H) {
       for (int m = 0; m < K0e; ++m) {
@@ -413,7 +406,7 @@ __global__ void k_spec_z(const float2* __restrict__ t2, void* __restrict__ spec,
         acc = cadd(acc, cmul(v, tw0[(int)(((long long)kz * p) % P0)]));
       }
     }
-    if (real_out)
+    if (mode == SPEC_REAL_EVEN)
       ((float*)spec)[i] = acc.x;
     else
       ((float2*)spec)[i] = acc;
@@ -439,8 +432,10 @@ struct pvd_plan {
   float2* buf1 = nullptr;
   float2* buf2 = nullptr;
   float2* buf3[PVD_MAX_KERNELS] = {};
+  const FastLen* fl[3] = {nullptr, nullptr, nullptr};  // register four-step kernels per axis (or generic)
   void* spec[PVD_MAX_KERNELS] = {};
-  int spec_real[PVD_MAX_KERNELS] = {};
+  int spec_mode[PVD_MAX_KERNELS] = {};
+  size_t spec_bytes[PVD_MAX_KERNELS] = {};
   int spec_set[PVD_MAX_KERNELS] = {};
   size_t ws_bytes = 0;
   size_t smem_x = 0, smem_y = 0, smem_z = 0;
@@ -527,7 +522,15 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
     p->N[i] = d->n[i];
     p->kmax[i] = d->kmax[i];
     int need = (d->mode == PVD_MODE_LINEAR) ? d->n[i] + d->kmax[i] - 1 : d->n[i];
-    int L = d->pad[i] ? d->pad[i] : (d->mode == PVD_MODE_LINEAR ? next_smooth7(need) : need);
+    int L = d->pad[i];
+    if (!L) {
+      if (d->mode == PVD_MODE_CIRCULAR) {
+        L = need;
+      } else {  // prefer a length with register four-step kernels when it pads by <= 25 %
+        const int lf = fast_len_at_least(need), ls = next_smooth7(need);
+        L = (lf && (lf == ls || 4 * lf <= 5 * need)) ? lf : ls;
+      }
+    }
     if (L < need || (d->mode == PVD_MODE_CIRCULAR && L != need)) {
       delete p;
       return set_error(PVD_ERR_ARG, "pvd_plan_create: explicit pad too small (LINEAR needs n+kmax-1, CIRCULAR needs n)");
@@ -538,6 +541,7 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
                                                 " has a prime factor > 7 (CIRCULAR mode needs 7-smooth dims)");
     }
     p->P[i] = L;
+    p->fl[i] = fast_len(L);
   }
   p->H = p->P[2] / 2 + 1;
   p->HS = (p->H + TX - 1) / TX * TX;
@@ -546,7 +550,10 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
   p->smem_z = smem_bytes(p->P[0], p->nk > 1 ? 3 : 2);
   int smem_max = 0;
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->dev);
-  if ((int)std::max({p->smem_x, p->smem_y, p->smem_z}) > smem_max) {
+  const size_t need_x = p->fl[2] ? p->fl[2]->smem_row : p->smem_x;
+  const size_t need_y = p->fl[1] ? p->fl[1]->smem_col : p->smem_y;
+  const size_t need_z = p->fl[0] ? p->fl[0]->smem_col : p->smem_z;
+  if ((int)std::max({need_x, need_y, need_z}) > smem_max) {
     delete p;
     return set_error(PVD_ERR_UNSUPPORTED, "pvd_plan_create: FFT length too large for one shared-memory tile");
   }
@@ -555,6 +562,15 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
   cudaFuncSetAttribute(k_y<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
   cudaFuncSetAttribute(k_y<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
   cudaFuncSetAttribute(k_z, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  for (int i = 0; i < 3; ++i) {
+    const FastLen* f = p->fl[i];
+    if (!f) continue;
+    cudaFuncSetAttribute((const void*)f->x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+    cudaFuncSetAttribute((const void*)f->x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+    cudaFuncSetAttribute((const void*)f->y_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+    cudaFuncSetAttribute((const void*)f->y_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+    cudaFuncSetAttribute((const void*)f->z, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  }
 
   pvd_status st = PVD_OK;
   // twiddle tables exp(-2 pi i n / L), computed in FP64 on the host
@@ -575,13 +591,11 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
   }
   const size_t b1 = sizeof(float2) * (size_t)p->N[0] * p->N[1] * p->HS;
   const size_t b2 = sizeof(float2) * (size_t)p->N[0] * p->P[1] * p->HS;
-  const size_t sp = (size_t)p->P[0] * p->P[1] * p->HS;
   void* ptr = nullptr;
   if (st == PVD_OK) st = plan_alloc(p, b1, &ptr), p->buf1 = (float2*)ptr;
   if (st == PVD_OK) st = plan_alloc(p, b2, &ptr), p->buf2 = (float2*)ptr;
   if (st == PVD_OK) p->buf3[0] = p->buf2;  // slot 0 transforms in place
   for (int s = 1; s < p->nk && st == PVD_OK; ++s) st = plan_alloc(p, b2, &ptr), p->buf3[s] = (float2*)ptr;
-  for (int s = 0; s < p->nk && st == PVD_OK; ++s) st = plan_alloc(p, sizeof(float2) * sp, &ptr), p->spec[s] = ptr;
   if (st == PVD_OK) {
     // padding columns [H, HS) are carried through the column passes; keep them defined
     cudaError_t e = cudaMemset(p->buf1, 0, b1);
@@ -628,7 +642,9 @@ extern "C" pvd_status pvd_plan_set_kernel(pvd_plan* p, int slot, const double* k
     if (!std::isfinite(kh[i]))
       return set_error(PVD_ERR_NUMERIC, "pvd_plan_set_kernel: kernel has a non-finite value at flat index " +
                                             std::to_string(i));
-  // placement offsets and symmetry (real spectrum) detection
+  // placement offsets; a LINEAR-mode kernel with odd dims that is even along
+  // every axis separately (any radial kernel) has a real spectrum that is even
+  // in kz and ky: only a quarter of it is stored.
   int o[3], Ke[3];
   bool sym = (p->mode == PVD_MODE_LINEAR);
   for (int i = 0; i < 3; ++i) {
@@ -638,9 +654,14 @@ extern "C" pvd_status pvd_plan_set_kernel(pvd_plan* p, int slot, const double* k
   }
   for (long long i = 0; sym && i < nk; ++i) {
     const int a = (int)(i / ((long long)k1 * k2)), b = (int)((i / k2) % k1), c = (int)(i % k2);
-    const long long j = ((long long)(k0 - 1 - a) * k1 + (k1 - 1 - b)) * k2 + (k2 - 1 - c);
-    if (kh[i] != kh[j]) sym = false;
+    const long long jz = ((long long)(k0 - 1 - a) * k1 + b) * k2 + c;
+    const long long jy = ((long long)a * k1 + (k1 - 1 - b)) * k2 + c;
+    const long long jx = ((long long)a * k1 + b) * k2 + (k2 - 1 - c);
+    if (kh[i] != kh[jz] || kh[i] != kh[jy] || kh[i] != kh[jx]) sym = false;
   }
+  const int smode = sym ? SPEC_REAL_EVEN : SPEC_COMPLEX;
+  const size_t spec_bytes = sym ? sizeof(float) * (size_t)(p->P[0] / 2 + 1) * (p->P[1] / 2 + 1) * p->HS
+                                : sizeof(float2) * (size_t)p->P[0] * p->P[1] * p->HS;
   const double inv_p = 1.0 / ((double)p->P[0] * p->P[1] * p->P[2]);
 
   double* kd = nullptr;
@@ -665,6 +686,27 @@ extern "C" pvd_status pvd_plan_set_kernel(pvd_plan* p, int slot, const double* k
     cudaGetLastError();
     cleanup();
     return cuda_error(e, "cudaMalloc(kernel staging)");
+  }
+  if (p->spec[slot]) {  // replace the slot's previous spectrum
+    for (auto it = p->allocs.begin(); it != p->allocs.end(); ++it)
+      if (*it == p->spec[slot]) {
+        p->allocs.erase(it);
+        break;
+      }
+    cudaFree(p->spec[slot]);
+    p->ws_bytes -= p->spec_bytes[slot];
+    p->spec[slot] = nullptr;
+    p->spec_set[slot] = 0;
+  }
+  {
+    void* sp = nullptr;
+    pvd_status as = plan_alloc(p, spec_bytes, &sp);
+    if (as != PVD_OK) {
+      cleanup();
+      return as;
+    }
+    p->spec[slot] = sp;
+    p->spec_bytes[slot] = spec_bytes;
   }
   e = cudaMemcpy(kd, kh, sizeof(double) * nk, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
@@ -693,14 +735,14 @@ extern "C" pvd_status pvd_plan_set_kernel(pvd_plan* p, int slot, const double* k
   count_launch();
   k_spec_y<<<gs, NT>>>(t1, t2, k0, k1, Ke[1], o[1], p->P[1], p->H, p->tw[1]);
   count_launch();
-  k_spec_z<<<gs, NT>>>(t2, p->spec[slot], sym ? 1 : 0, Ke[0], o[0], p->P[0], p->P[1], p->H, p->HS, p->tw[0]);
+  k_spec_z<<<gs, NT>>>(t2, p->spec[slot], smode, Ke[0], o[0], p->P[0], p->P[1], p->H, p->HS, p->tw[0]);
   count_launch();
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e != cudaSuccess) st = cuda_error(e, "kernel spectrum");
   cleanup();
   if (st == PVD_OK) {
-    p->spec_real[slot] = sym ? 1 : 0;
+    p->spec_mode[slot] = smode;
     p->spec_set[slot] = 1;
   }
   return st;
@@ -719,40 +761,71 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
   const int xblocks = (nrows + 2 * TX - 1) / (2 * TX);
   const int ctiles = p->HS / TX;
 
+  const FastLen* fx = p->fl[2];
+  const FastLen* fy = p->fl[1];
+  const FastLen* fz = p->fl[0];
   {
     PassTimer t(p, 0, st);
-    k_x_fwd<<<xblocks, NT, p->smem_x, st>>>(in, p->buf1, nrows, N2, p->HS, p->f[2], p->tw[2]);
-    PVD_LAUNCH_CHECK("k_x_fwd");
+    if (fx)
+      fx->x_fwd<<<xblocks, fx->threads, fx->smem_row, st>>>(in, p->buf1, nrows, N2, p->HS, p->tw[2]);
+    else
+      k_x_fwd<<<xblocks, NT, p->smem_x, st>>>(in, p->buf1, nrows, N2, p->HS, p->f[2], p->tw[2]);
+    PVD_LAUNCH_CHECK("x_fwd");
   }
   {
     PassTimer t(p, 1, st);
-    k_y<false><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf1, p->buf2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
-    PVD_LAUNCH_CHECK("k_y<fwd>");
+    if (fy)
+      fy->y_fwd<<<dim3(ctiles, N0), fy->threads, fy->smem_col, st>>>(p->buf1, p->buf2, N1, p->P[1], p->HS, p->tw[1]);
+    else
+      k_y<false><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf1, p->buf2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
+    PVD_LAUNCH_CHECK("y_fwd");
   }
-  OutSet os;
-  std::memset(&os, 0, sizeof(os));
-  os.n = p->nk;
-  for (int s = 0; s < p->nk; ++s) {
-    os.p[s] = p->buf3[s];
-    os.s[s] = p->spec[s];
-    os.real[s] = p->spec_real[s];
-  }
-  {
+  // z pass: the fast kernel takes up to FZ_SLOTS kernel slots per launch (each
+  // launch reads the forward data again); the generic one takes all of them.
+  // Slot 0 transforms in place, so it goes last.
+  const int group = fz ? FZ_SLOTS : PVD_MAX_KERNELS;
+  int order[PVD_MAX_KERNELS];
+  for (int s = 0; s < p->nk; ++s) order[s] = (s + 1) % p->nk;
+  for (int g0 = 0; g0 < p->nk; g0 += group) {
+    OutSet os;
+    std::memset(&os, 0, sizeof(os));
+    os.n = std::min(group, p->nk - g0);
+    os.P0 = p->P[0];
+    os.P0h = p->P[0] / 2 + 1;
+    os.P1h = p->P[1] / 2 + 1;
+    for (int i = 0; i < os.n; ++i) {
+      const int s = (p->nk <= group) ? i : order[g0 + i];
+      os.p[i] = p->buf3[s];
+      os.s[i] = p->spec[s];
+      os.mode[i] = p->spec_mode[s];
+    }
     PassTimer t(p, 2, st);
-    k_z<<<dim3(ctiles, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
-    PVD_LAUNCH_CHECK("k_z");
+    if (fz)
+      fz->z<<<dim3(ctiles, p->P[1]), fz->threads, fz->smem_col, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->tw[0]);
+    else
+      k_z<<<dim3(ctiles, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
+    PVD_LAUNCH_CHECK("z");
   }
   for (int s = 0; s < p->nk; ++s) {
     {
       PassTimer t(p, 3, st);
-      k_y<true><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS, p->f[1], p->tw[1]);
-      PVD_LAUNCH_CHECK("k_y<inv>");
+      if (fy)
+        fy->y_inv<<<dim3(ctiles, N0), fy->threads, fy->smem_col, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS,
+                                                                       p->tw[1]);
+      else
+        k_y<true><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS, p->f[1],
+                                                           p->tw[1]);
+      PVD_LAUNCH_CHECK("y_inv");
     }
     {
       PassTimer t(p, 4, st);
-      k_x_inv<<<xblocks, NT, p->smem_x, st>>>(p->buf1, dose + s * vox, rho, nrows, N2, p->HS, out_scale, p->f[2],
-                                             p->tw[2]);
-      PVD_LAUNCH_CHECK("k_x_inv");
+      if (fx)
+        fx->x_inv<<<xblocks, fx->threads, fx->smem_row, st>>>(p->buf1, dose + s * vox, rho, nrows, N2, p->HS,
+                                                               out_scale, p->tw[2]);
+      else
+        k_x_inv<<<xblocks, NT, p->smem_x, st>>>(p->buf1, dose + s * vox, rho, nrows, N2, p->HS, out_scale, p->f[2],
+                                               p->tw[2]);
+      PVD_LAUNCH_CHECK("x_inv");
     }
   }
   return PVD_OK;

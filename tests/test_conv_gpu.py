@@ -134,3 +134,36 @@ def test_errors_are_raised_not_faulted():
             p.set_kernel(0, np.full((3, 3, 3), np.nan))
         with pytest.raises(PvdError, match="NUMERIC"):
             p.set_kernel(0, np.zeros((3, 3, 3)), normalize=True)
+
+
+def _fast_lengths():
+    from pyvoxeldosimetry_gb300 import _native
+    return _native.fast_lengths()
+
+
+@pytest.mark.parametrize("L", [64, 72, 80, 96, 112, 128, 144, 160, 192, 224, 240, 256, 280, 288, 320, 336, 384,
+                               400, 448, 512, 560, 576, 640])
+def test_every_fast_length_on_every_axis(L):
+    """Force FFT length L on all three axes (small volume): exercises the register
+    four-step x/y/z pass kernels of that length with a real-even (radial) kernel
+    and a complex-spectrum (asymmetric) kernel in one plan."""
+    assert L in _fast_lengths()
+    rng = np.random.default_rng(L)
+    shape = (min(L - 8, 37), min(L - 8, 20), min(L - 8, 45))
+    a = rng.random(shape)
+    ks = [radial_kernel(9, 1.8, 1.5), rng.random((5, 7, 3))]
+    d = run_plan(a, ks, pad=(L, L, L))
+    for s, k in enumerate(ks):
+        assert rel_err(d[s], oc.linear_conv_same(a, k)) <= TOL
+
+
+def test_fast_full_extent_and_many_slots():
+    """N = P - K + 1 on the 280 axis (no slack in the padding) and more kernel slots
+    than one fast z launch takes (slot 0 transforms in place and must run last)."""
+    rng = np.random.default_rng(21)
+    shape = (260, 12, 24)
+    a = rng.random(shape)
+    ks = [radial_kernel(21, 1.8, 1.5)] + [rng.random((3, 3, 3)) for _ in range(5)] + [radial_kernel(11, 0.5, 1.5)]
+    d = run_plan(a, ks, pad=(280, 64, 64))
+    for s, k in enumerate(ks):
+        assert rel_err(d[s], oc.linear_conv_same(a, k)) <= TOL

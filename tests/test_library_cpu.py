@@ -34,3 +34,14 @@ def test_errors_without_gpu_are_status_codes():
     assert lib.pvd_plan_create(None, None) == 1
     assert _native.last_error().startswith("pvd_plan_create")
     assert lib.pvd_conv_execute(None, None, None, None, ctypes.c_float(1.0), None) == 1
+
+
+def test_fast_length_registry():
+    lens = _native.fast_lengths()
+    assert lens == sorted(lens) and 280 in lens and 144 in lens
+    for L in lens:
+        r = L
+        for p in (2, 3, 5, 7):
+            while r % p == 0:
+                r //= p
+        assert r == 1
