@@ -168,15 +168,18 @@ pvd_status pvd_weighted_sum(const float* const* maps, const float* weights, int 
  * Residuals are weights[k] * (f(t_k) - y_k) (curve_fit with sigma = 1/weights;
  * weights may be NULL = 1).  acts_d: device float32 [n_times][n_vox];
  * params_d: device float64 [n_par][n_vox]; auc_d: device float64 [n_vox];
- * ok_d: device uint8 [n_vox] (1 = converged) or NULL.  max_iter bounds the
- * Levenberg-Marquardt iterations (non-convergence is a failure). */
+ * ok_d: device uint8 [n_vox] (1 = converged) or NULL.  The minimiser is
+ * Moré's scaled trust-region Levenberg-Marquardt (the algorithm of MINPACK
+ * lmdif, which curve_fit runs); max_fev is curve_fit's maxfev (model
+ * evaluations, a Jacobian counting n_par of them) and, as there, running out
+ * of it or of attainable precision is a failure. */
 enum {
   PVD_FIT_MONO_LAMBDA = 0, PVD_FIT_F2 = 1, PVD_FIT_F3 = 2, PVD_FIT_F3A = 3, PVD_FIT_F4A = 4,
   PVD_FIT_F4B = 5, PVD_FIT_F4C = 6, PVD_FIT_LM_MONO = 7, PVD_FIT_LM_BI = 8, PVD_FIT_LM_TRI = 9
 };
 enum { PVD_FIT_FORCE_ZERO_AT_T0 = 1, PVD_FIT_P0_GIVEN = 2 };
 pvd_status pvd_tac_fit(int model, const double* times, const double* weights, int n_times,
-                       const double* p0, double lam_phys, double auc_limit, int max_iter, int flags,
+                       const double* p0, double lam_phys, double auc_limit, int max_fev, int flags,
                        const float* acts_d, long long n_vox, double* params_d, double* auc_d,
                        unsigned char* ok_d, pvd_stream stream);
 

@@ -552,7 +552,7 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->dev);
   const size_t need_x = p->fl[2] ? p->fl[2]->smem_row : p->smem_x;
   const size_t need_y = p->fl[1] ? p->fl[1]->smem_col : p->smem_y;
-  const size_t need_z = p->fl[0] ? p->fl[0]->smem_col : p->smem_z;
+  const size_t need_z = p->fl[0] ? p->fl[0]->smem_z : p->smem_z;
   if ((int)std::max({need_x, need_y, need_z}) > smem_max) {
     delete p;
     return set_error(PVD_ERR_UNSUPPORTED, "pvd_plan_create: FFT length too large for one shared-memory tile");
@@ -801,7 +801,7 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
     }
     PassTimer t(p, 2, st);
     if (fz)
-      fz->z<<<dim3(ctiles, p->P[1]), fz->threads, fz->smem_col, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->tw[0]);
+      fz->z<<<dim3(ctiles, p->P[1]), fz->threads, fz->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->tw[0]);
     else
       k_z<<<dim3(ctiles, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
     PVD_LAUNCH_CHECK("z");

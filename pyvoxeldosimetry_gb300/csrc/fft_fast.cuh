@@ -28,7 +28,7 @@ typedef void (*KzFn)(const float2*, OutSet, int, int, int, const float2*);
 
 struct FastLen {
   int L, A, B, threads;
-  size_t smem_col, smem_row;
+  size_t smem_col, smem_row, smem_z;
   KxFwdFn x_fwd;
   KxInvFn x_inv;
   KyFn y_fwd, y_inv;
@@ -82,13 +82,18 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_y(const float2* __restrict
 // z pass: forward, spectrum multiply, inverse, crop — every kernel slot.
 // blockIdx.x = column tile, blockIdx.y = ky.
 // ---------------------------------------------------------------------------
+// 3 resident CTAs per SM where the register arrays allow it without spilling
+// (A + B <= 36: at most 64 registers at 320 threads); the compiler's choice otherwise
+__host__ __device__ constexpr int z_min_blocks(int a, int b) { return (a + b <= 36 && cmax(a, b) <= 20) ? 3 : 1; }
+
 template <int A, int B>
-__global__ void __launch_bounds__(FTX* cmax(A, B)) kf_z(const float2* __restrict__ in, OutSet os, int N0, int P1,
+__global__ void __launch_bounds__(FTX* cmax(A, B), z_min_blocks(A, B)) kf_z(const float2* __restrict__ in, OutSet os, int N0, int P1,
                                                          int HS, const float2* __restrict__ twg) {
   constexpr int L = A * B, NTH = FTX * cmax(A, B);
   extern __shared__ float2 sm[];
   float2* tw = sm;
   float2* ex = sm + tw_slots(L);
+  float2* xs = ex + L * FTX;  // forward spectrum of the tile, kept for every slot
   const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
   const int kx0 = blockIdx.x * FTX;
   const int ky = blockIdx.y;
@@ -104,15 +109,28 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_z(const float2* __restrict
   }
   load_tw<L>(tw, twg, NTH);
   __syncthreads();
-  float2 X[A];
-  four_step<A, B, false, FTX, false>(v, X, ex, tw, c, j);
-  // kernel slots [s0, s0 + FZ_SLOTS) of this launch, unrolled so the slot
-  // arguments stay in the parameter bank
+  {
+    float2 X[A];
+    four_step<A, B, false, FTX, false>(v, X, ex, tw, c, j);
+    if (j < B) {
+      static_for<A>([&](auto iq) {
+        constexpr int q = decltype(iq)::value;
+        xs[(j + B * q) * FTX + c] = X[q];
+      });
+    }
+  }
+  // kernel slots of this launch, unrolled so the slot arguments stay in the
+  // parameter bank; the forward spectrum is re-read from shared memory per
+  // slot (each thread reads back what it wrote), which keeps registers low
   static_for<FZ_SLOTS>([&](auto is) {
     constexpr int sl = decltype(is)::value;
     if (sl < os.n) {
-      float2 Y[A];
+      float2 X[A], Y[A];
       if (j < B) {
+        static_for<A>([&](auto iq) {
+          constexpr int q = decltype(iq)::value;
+          X[q] = xs[(j + B * q) * FTX + c];
+        });
         if (os.mode[sl] == SPEC_REAL_EVEN) {
           const float* S = (const float*)os.s[sl];
           static_for<A>([&](auto iq) {
@@ -146,45 +164,68 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_z(const float2* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// x forward: weighted timepoint sum, zero pad, R2C of 2*FTX real rows packed
-// as FTX complex rows, written as [row][HS] half spectra.
+// Row passes (x axis, contiguous).  A CTA owns ROWS = 2*FTX consecutive rows:
+// a contiguous block of global memory, moved with fully coalesced loads that
+// keep XU loads per thread in flight.  Shared tiles use odd row strides so the
+// transposed per-transform reads of the four-step FFT are bank-conflict free.
+// Real rows 2m and 2m+1 form the real and imaginary part of transform m.
 // ---------------------------------------------------------------------------
+constexpr int XU = 8;
+
+// x forward: weighted timepoint sum, zero pad, R2C, half spectra [row][HS].
 template <int A, int B>
 __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_fwd(ActIn in, float2* __restrict__ out, int nrows, int N2,
                                                              int HS, const float2* __restrict__ twg) {
-  constexpr int L = A * B, NTH = FTX * cmax(A, B), H = L / 2 + 1;
+  constexpr int L = A * B, NTH = FTX * cmax(A, B), H = L / 2 + 1, ROWS = 2 * FTX;
+  constexpr int NWF = NTH / 32;  // full warps (the last warp is partial when max(A, B) is odd)
+  constexpr int S2 = L | 1;  // odd float2 stride of the spectrum tile
   extern __shared__ float2 sm[];
   float2* tw = sm;
-  float2* buf = sm + tw_slots(L);  // [L][FTXP] staging, also the exchange tile
-  const long long row0 = (long long)blockIdx.x * (2 * FTX);
+  float2* buf = sm + tw_slots(L);               // chunk / exchange / spectrum tile (aliased in turn)
+  float* chunk = reinterpret_cast<float*>(buf);  // [ROWS][S] real rows
+  const int S = N2 | 1;
+  const long long row0 = (long long)blockIdx.x * ROWS;
+  const int nr = (int)min((long long)ROWS, (long long)nrows - row0);
   load_tw<L>(tw, twg, NTH);
-  for (int idx = threadIdx.x; idx < FTX * L; idx += NTH) {
-    const int m = idx / L, n = idx - m * L;
-    float2 val = make_float2(0.f, 0.f);
-    if (n < N2) {
-      const long long ra = row0 + 2 * m, rb = ra + 1;
-      if (ra < nrows) {
-        const long long o = ra * N2 + n;
-        float s = 0.f;
-        for (int t = 0; t < in.n; ++t) s += in.w[t] * __ldg(in.p[t] + o);
-        val.x = s;
-      }
-      if (rb < nrows) {
-        const long long o = rb * N2 + n;
-        float s = 0.f;
-        for (int t = 0; t < in.n; ++t) s += in.w[t] * __ldg(in.p[t] + o);
-        val.y = s;
+  // whole warps take whole rows: lane-contiguous loads, XU per lane in flight
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < NWF) {
+    for (int rr = warp; rr < nr; rr += NWF) {
+      for (int n0 = 0; n0 < N2; n0 += 32 * XU) {
+        float r[XU];
+#pragma unroll
+        for (int u = 0; u < XU; ++u) r[u] = 0.f;
+        for (int t = 0; t < in.n; ++t) {
+          const float* src = in.p[t] + (row0 + rr) * N2;
+          const float w = in.w[t];
+#pragma unroll
+          for (int u = 0; u < XU; ++u) {
+            const int n = n0 + 32 * u + lane;
+            if (n < N2) r[u] += w * __ldg(src + n);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < XU; ++u) {
+          const int n = n0 + 32 * u + lane;
+          if (n < N2) chunk[rr * S + n] = r[u];
+        }
       }
     }
-    buf[n * FTXP + m] = val;
   }
   __syncthreads();
   const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
   float2 v[B];
   if (j < A) {
+    const bool va = 2 * c < nr, vb = 2 * c + 1 < nr;
     static_for<B>([&](auto ib) {
       constexpr int b = decltype(ib)::value;
-      v[b] = buf[(j + A * b) * FTXP + c];
+      const int n = j + A * b;
+      float xa = 0.f, xb = 0.f;
+      if (n < N2) {
+        if (va) xa = chunk[(2 * c) * S + n];
+        if (vb) xb = chunk[(2 * c + 1) * S + n];
+      }
+      v[b] = make_float2(xa, xb);
     });
   }
   float2 X[A];
@@ -193,54 +234,82 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_fwd(ActIn in, float2* __
   if (j < B) {
     static_for<A>([&](auto iq) {
       constexpr int q = decltype(iq)::value;
-      buf[(j + B * q) * FTXP + c] = X[q];
+      buf[c * S2 + j + B * q] = X[q];
     });
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < FTX * H; idx += NTH) {
-    const int m = idx / H, k = idx - m * H;
-    const long long ra = row0 + 2 * m, rb = ra + 1;
-    const int kk = (k == 0) ? 0 : L - k;
-    const float2 z1 = buf[k * FTXP + m];
-    const float2 z2 = buf[kk * FTXP + m];
-    if (ra < nrows) out[ra * HS + k] = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
-    if (rb < nrows) out[rb * HS + k] = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
+  if (warp < NWF) {
+    for (int rr = warp; rr < nr; rr += NWF) {
+      const int m = rr >> 1;
+      const bool odd = rr & 1;
+      float2* dst = out + (row0 + rr) * HS;
+      for (int k = lane; k < H; k += 32) {
+        const float2 z1 = buf[m * S2 + k];
+        const float2 z2 = buf[m * S2 + (k ? L - k : 0)];
+        // Xa = (Z[k] + conj Z[-k]) / 2 ;  Xb = (Z[k] - conj Z[-k]) / (2i)
+        dst[k] = odd ? make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x))
+                     : make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+      }
+    }
   }
 }
 
-// ---------------------------------------------------------------------------
 // x inverse: C2R of pairs of half-spectrum rows, crop, scale, density.
-// ---------------------------------------------------------------------------
 template <int A, int B>
 __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_inv(const float2* __restrict__ in, float* __restrict__ out,
                                                              const float* __restrict__ rho, int nrows, int N2, int HS,
                                                              float scale, const float2* __restrict__ twg) {
-  constexpr int L = A * B, NTH = FTX * cmax(A, B), H = L / 2 + 1;
+  constexpr int L = A * B, NTH = FTX * cmax(A, B), H = L / 2 + 1, ROWS = 2 * FTX;
+  constexpr int NWF = NTH / 32;  // full warps (the last warp is partial when max(A, B) is odd)
+  constexpr int S2 = H | 1;  // odd float2 stride of the half-spectrum tiles
   extern __shared__ float2 sm[];
   float2* tw = sm;
   float2* buf = sm + tw_slots(L);
-  const long long row0 = (long long)blockIdx.x * (2 * FTX);
+  float2* ha = buf;              // even rows  [FTX][S2]
+  float2* hb = buf + FTX * S2;   // odd rows   [FTX][S2]
+  float* oc = reinterpret_cast<float*>(buf);  // output rows [ROWS][S] (aliases the tiles later)
+  const int S = N2 | 1;
+  const long long row0 = (long long)blockIdx.x * ROWS;
+  const int nr = (int)min((long long)ROWS, (long long)nrows - row0);
   load_tw<L>(tw, twg, NTH);
-  for (int idx = threadIdx.x; idx < FTX * H; idx += NTH) {
-    const int m = idx / H, k = idx - m * H;
-    const long long ra = row0 + 2 * m, rb = ra + 1;
-    float2 xa = (ra < nrows) ? in[ra * HS + k] : make_float2(0.f, 0.f);
-    float2 xb = (rb < nrows) ? in[rb * HS + k] : make_float2(0.f, 0.f);
-    if (k == 0 || 2 * k == L) {
-      xa.y = 0.f;
-      xb.y = 0.f;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp < NWF) {
+    for (int rr = warp; rr < nr; rr += NWF) {
+      const float2* src = in + (row0 + rr) * HS;
+      float2* dsm = ((rr & 1) ? hb : ha) + (rr >> 1) * S2;
+      for (int k0 = 0; k0 < H; k0 += 32 * XU) {
+        float2 r[XU];
+#pragma unroll
+        for (int u = 0; u < XU; ++u) {
+          const int k = k0 + 32 * u + lane;
+          if (k < H) r[u] = src[k];
+        }
+#pragma unroll
+        for (int u = 0; u < XU; ++u) {
+          const int k = k0 + 32 * u + lane;
+          if (k < H) dsm[k] = r[u];
+        }
+      }
     }
-    buf[k * FTXP + m] = make_float2(xa.x - xb.y, xa.y + xb.x);
-    const int kk = L - k;
-    if (k > 0 && kk >= H) buf[kk * FTXP + m] = make_float2(xa.x + xb.y, xb.x - xa.y);
   }
   __syncthreads();
   const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
   float2 v[B];
   if (j < A) {
+    const bool va = 2 * c < nr, vb = 2 * c + 1 < nr;
     static_for<B>([&](auto ib) {
       constexpr int b = decltype(ib)::value;
-      v[b] = buf[(j + A * b) * FTXP + c];
+      const int n = j + A * b;
+      const bool lo = n < H;
+      const int k = lo ? n : L - n;
+      float2 xa = va ? ha[c * S2 + k] : make_float2(0.f, 0.f);
+      float2 xb = vb ? hb[c * S2 + k] : make_float2(0.f, 0.f);
+      if (k == 0 || 2 * k == L) {  // DC / Nyquist bins of a real row are real
+        xa.y = 0.f;
+        xb.y = 0.f;
+      }
+      // Z[n] = Xa[n] + i Xb[n] for n < H, conj Xa[L-n] + i conj Xb[L-n] above
+      v[b] = lo ? make_float2(xa.x - xb.y, xa.y + xb.x) : make_float2(xa.x + xb.y, xb.x - xa.y);
     });
   }
   float2 X[A];
@@ -249,29 +318,37 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_inv(const float2* __rest
   if (j < B) {
     static_for<A>([&](auto iq) {
       constexpr int q = decltype(iq)::value;
-      buf[(j + B * q) * FTXP + c] = X[q];
+      const int n = j + B * q;
+      if (n < N2) {
+        oc[(2 * c) * S + n] = X[q].x * scale;
+        oc[(2 * c + 1) * S + n] = X[q].y * scale;
+      }
     });
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < FTX * N2; idx += NTH) {
-    const int m = idx / N2, n = idx - m * N2;
-    const long long ra = row0 + 2 * m, rb = ra + 1;
-    const float2 z = buf[n * FTXP + m];
-    if (ra < nrows) {
-      float val = z.x * scale;
-      if (rho) {
-        const float d = __ldg(rho + ra * N2 + n);
-        val = (d > 0.f) ? val / d : 0.f;
+  if (warp < NWF) {
+    for (int rr = warp; rr < nr; rr += NWF) {
+      float* dst = out + (row0 + rr) * N2;
+      const float* dr = rho ? rho + (row0 + rr) * N2 : nullptr;
+      for (int n0 = 0; n0 < N2; n0 += 32 * XU) {
+        float d[XU];
+        if (dr) {
+#pragma unroll
+          for (int u = 0; u < XU; ++u) {
+            const int n = n0 + 32 * u + lane;
+            d[u] = (n < N2) ? __ldg(dr + n) : 1.f;
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < XU; ++u) {
+          const int n = n0 + 32 * u + lane;
+          if (n < N2) {
+            float val = oc[rr * S + n];
+            if (dr) val = (d[u] > 0.f) ? val / d[u] : 0.f;
+            dst[n] = val;
+          }
+        }
       }
-      out[ra * N2 + n] = val;
-    }
-    if (rb < nrows) {
-      float val = z.y * scale;
-      if (rho) {
-        const float d = __ldg(rho + rb * N2 + n);
-        val = (d > 0.f) ? val / d : 0.f;
-      }
-      out[rb * N2 + n] = val;
     }
   }
 }
@@ -285,6 +362,7 @@ FastLen make_fast_len() {
   f.B = B;
   f.threads = FTX * cmax(A, B);
   f.smem_col = sizeof(float2) * (size_t)(tw_slots(L) + L * FTX);
+  f.smem_z = sizeof(float2) * (size_t)(tw_slots(L) + 2 * L * FTX);
   f.smem_row = sizeof(float2) * (size_t)(tw_slots(L) + L * FTXP);
   f.x_fwd = kf_x_fwd<A, B>;
   f.x_inv = kf_x_inv<A, B>;

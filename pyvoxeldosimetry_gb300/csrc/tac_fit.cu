@@ -5,10 +5,12 @@
 //   TimeCurveFitting._calculate_accumulated_dose  (curve_fitting.py:74-84)
 //   TimeCurveFitting.fit_time_activity_curve_advanced (curve_fitting.py:112-219)
 // with the same models, initial guesses, sigma = 1/weight residual scaling,
-// failure fallbacks and AUC formulas.  The minimiser is a Levenberg-Marquardt
-// iteration with Marquardt's diagonal scaling and an analytic Jacobian (the
-// reference's MINPACK lmdif uses forward differences); both converge to the
-// same least-squares minimum on well-posed curves.  Non-finite samples or
+// failure fallbacks and AUC formulas.  The minimiser restates Moré's scaled
+// trust-region Levenberg-Marquardt (the published algorithm behind MINPACK
+// lmdif, which curve_fit runs) on the normal equations in FP64 with an
+// analytic Jacobian where lmdif uses forward differences; initial trust
+// region, scaling, step control, convergence tests and info codes follow the
+// algorithm, so success/failure match curve_fit's on the same curves.  Non-finite samples or
 // fewer samples than parameters are failures, as curve_fit raises for them.
 //
 // Layout: activities [T][n_vox] float32 (time-major, the stacked maps);
@@ -35,7 +37,7 @@ struct FitArgs {
   int T;
   double lam_phys;               // ln2 / physical half-life (models with lambda_phys)
   double auc_limit;              // mono-lambda model: integration limit (same time unit)
-  int max_iter;
+  int max_fev;                  // model-evaluation budget (curve_fit's maxfev)
   int force_zero_at_t0;
   int p0_from_data;              // mono-lambda: p0 = [y(t0), lam_phys] per voxel
 };
@@ -188,15 +190,15 @@ __device__ double cost_at(const FitArgs& a, const double* y, const double* p) {
   return 0.5 * cost;
 }
 
-// solve (A + mu diag(A)) h = -g by Cholesky (A symmetric, upper triangle stored); false if not SPD
+// Cholesky of (A + par diag(D^2)) (A symmetric, upper triangle stored in A[i*N+c], c >= i).
+// L is lower triangular, row major.  false if not positive definite.
 template <int N>
-__device__ bool damped_solve(const double* A, const double* g, double mu, double* h) {
-  double L[N * N];
+__device__ bool chol_damped(const double* A, const double* D, double par, double* L) {
 #pragma unroll
   for (int i = 0; i < N; ++i) {
 #pragma unroll
     for (int c = 0; c <= i; ++c) {
-      double s = (c == i) ? A[i * N + i] * (1.0 + mu) + 1e-300 : A[c * N + i];
+      double s = (c == i) ? A[i * N + i] + par * D[i] * D[i] : A[c * N + i];
       for (int k = 0; k < c; ++k) s -= L[i * N + k] * L[c * N + k];
       if (c == i) {
         if (!(s > 0.0)) return false;
@@ -206,77 +208,188 @@ __device__ bool damped_solve(const double* A, const double* g, double mu, double
       }
     }
   }
-  double z[N];
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    double s = -g[i];
-    for (int k = 0; k < i; ++k) s -= L[i * N + k] * z[k];
-    z[i] = s / L[i * N + i];
-  }
-#pragma unroll
-  for (int i = N - 1; i >= 0; --i) {
-    double s = z[i];
-    for (int k = i + 1; k < N; ++k) s -= L[k * N + i] * h[k];
-    h[i] = s / L[i * N + i];
-  }
   return true;
 }
 
-// Levenberg-Marquardt from p (in/out); returns true on convergence.
-template <int M>
-__device__ bool lm_fit(const FitArgs& a, const double* y, double* p) {
-  constexpr int N = ModelTraits<M>::N;
-  double A[N * N], g[N], h[N], pn[N];
-  double F = normal_eq<M>(a, y, p, A, g);
-  if (!isfinite(F)) return false;
-  double mu = 1e-3;
-  double nu = 2.0;
-  for (int it = 0; it < a.max_iter; ++it) {
-    double gmax = 0.0, dmax = 0.0;
+template <int N>
+__device__ void chol_fwd(const double* L, const double* b, double* z) {  // L z = b
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      gmax = fmax(gmax, fabs(g[i]));
-      dmax = fmax(dmax, A[i * N + i]);
+  for (int i = 0; i < N; ++i) {
+    double s = b[i];
+    for (int k = 0; k < i; ++k) s -= L[i * N + k] * z[k];
+    z[i] = s / L[i * N + i];
+  }
+}
+
+template <int N>
+__device__ void chol_solve_neg(const double* L, const double* g, double* p) {  // L L^T p = -g
+  double z[N];
+  double mg[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) mg[i] = -g[i];
+  chol_fwd<N>(L, mg, z);
+#pragma unroll
+  for (int i = N - 1; i >= 0; --i) {
+    double s = z[i];
+    for (int k = i + 1; k < N; ++k) s -= L[k * N + i] * p[k];
+    p[i] = s / L[i * N + i];
+  }
+}
+
+template <int N>
+__device__ double dnorm(const double* D, const double* v) {
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) s += (D[i] * v[i]) * (D[i] * v[i]);
+  return sqrt(s);
+}
+
+// Trust-region step (Moré, "The Levenberg-Marquardt algorithm: implementation
+// and theory", 1978, the lmpar procedure) on the normal equations: find
+// par >= 0 with ||D p|| within 10 % of delta, p = -(A + par D^2)^-1 g, or the
+// Gauss-Newton step (par = 0) when it already fits in the region.
+template <int N>
+__device__ void lm_par(const double* A, const double* g, const double* D, double delta, double& par, double* p) {
+  const double dwarf = 2.2250738585072014e-308;
+  double L[N * N], w[N], q[N];
+  double parl = 0.0;
+  double fp;
+  if (chol_damped<N>(A, D, 0.0, L)) {
+    chol_solve_neg<N>(L, g, p);
+    const double dxn = dnorm<N>(D, p);
+    fp = dxn - delta;
+    if (fp <= 0.1 * delta) {
+      par = 0.0;
+      return;
     }
-    if (F == 0.0 || gmax == 0.0) return true;   // exact fit / stationary point
-    if (!damped_solve<N>(A, g, mu, h)) {
-      mu *= nu;
-      nu *= 2.0;
-      if (mu > 1e30) return false;
+#pragma unroll
+    for (int i = 0; i < N; ++i) q[i] = D[i] * (D[i] * p[i]) / dxn;
+    chol_fwd<N>(L, q, w);
+    double wn = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) wn += w[i] * w[i];
+    parl = (fp / delta) / wn;
+  }
+  double gn = 0.0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) gn += (g[i] / D[i]) * (g[i] / D[i]);
+  gn = sqrt(gn);
+  double paru = gn / delta;
+  if (paru == 0.0) paru = dwarf / fmin(delta, 0.1);
+  par = fmax(par, parl);
+  par = fmin(par, paru);
+  if (par == 0.0) par = gn / fmax(dnorm<N>(D, p), dwarf);
+  fp = 0.0;
+  for (int it = 1; it <= 10; ++it) {
+    if (par == 0.0) par = fmax(dwarf, 0.001 * paru);
+    if (!chol_damped<N>(A, D, par, L)) {  // only possible when D has zero entries
+      par = fmax(par * 10.0, dwarf);
       continue;
     }
-    double hn = 0.0, pnrm = 0.0;
+    chol_solve_neg<N>(L, g, p);
+    const double dxn = dnorm<N>(D, p);
+    const double temp = fp;
+    fp = dxn - delta;
+    if (fabs(fp) <= 0.1 * delta || (parl == 0.0 && fp <= temp && temp < 0.0) || it == 10) break;
 #pragma unroll
-    for (int i = 0; i < N; ++i) {
-      pn[i] = p[i] + h[i];
-      hn += h[i] * h[i];
-      pnrm += p[i] * p[i];
-    }
-    if (sqrt(hn) <= 1e-15 * (sqrt(pnrm) + 1e-300)) return true;
-    const double Fn = cost_at<M>(a, y, pn);
-    // predicted reduction of the damped quadratic model: 0.5 h^T (mu D h - g)
-    double pred = 0.0;
+    for (int i = 0; i < N; ++i) q[i] = D[i] * (D[i] * p[i]) / dxn;
+    chol_fwd<N>(L, q, w);
+    double wn = 0.0;
 #pragma unroll
-    for (int i = 0; i < N; ++i) pred += h[i] * (mu * A[i * N + i] * h[i] - g[i]);
-    pred *= 0.5;
-    const double rho = (F - Fn) / pred;
-    if (isfinite(Fn) && Fn < F && pred > 0.0) {
-      const double rel = (F - Fn) / F;
-#pragma unroll
-      for (int i = 0; i < N; ++i) p[i] = pn[i];
-      const double Fold = F;
-      F = normal_eq<M>(a, y, p, A, g);
-      const double t = 2.0 * rho - 1.0;
-      mu *= fmax(1.0 / 3.0, 1.0 - t * t * t);
-      nu = 2.0;
-      if (rel <= 1e-15 || Fold - F <= 1e-15 * Fold) return true;
-    } else {
-      mu *= nu;
-      nu *= 2.0;
-      if (mu > 1e30) return true;  // no further decrease possible: at the minimum to working precision
-    }
+    for (int i = 0; i < N; ++i) wn += w[i] * w[i];
+    const double parc = (fp / delta) / wn;
+    if (fp > 0.0) parl = fmax(parl, par);
+    if (fp < 0.0) paru = fmin(paru, par);
+    par = fmax(parl, par + parc);
   }
-  return false;
+}
+
+// Moré's Levenberg-Marquardt outer iteration (scaled trust region) with an
+// analytic Jacobian.  Returns MINPACK's info code: 1-4 success (ftol / xtol /
+// both / gtol), 5 evaluation budget exhausted, 6-8 tolerances too small, -1
+// non-finite cost.  `maxfev` counts model evaluations as a forward-difference
+// Jacobian would (N per Jacobian), so the budget matches curve_fit's.
+template <int M>
+__device__ int lm_fit(const FitArgs& a, const double* y, double* x, int maxfev) {
+  constexpr int N = ModelTraits<M>::N;
+  const double ftol = 1.49012e-8, xtol = 1.49012e-8, epsmch = 2.220446049250313e-16;
+  double A[N * N], g[N], D[N], p[N], xt[N];
+  int nfev = 1;
+  double fnorm = sqrt(2.0 * cost_at<M>(a, y, x));
+  if (!isfinite(fnorm)) return -1;
+  double delta = 0.0, xnorm = 0.0, par = 0.0;
+  for (int iter = 1;; ++iter) {
+    normal_eq<M>(a, y, x, A, g);
+    nfev += N;
+    double acn[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) acn[j] = sqrt(A[j * N + j]);
+    if (iter == 1) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) D[j] = (acn[j] == 0.0) ? 1.0 : acn[j];
+      xnorm = dnorm<N>(D, x);
+      delta = 100.0 * xnorm;
+      if (delta == 0.0) delta = 100.0;
+    }
+    double gnorm = 0.0;
+    if (fnorm != 0.0) {
+#pragma unroll
+      for (int j = 0; j < N; ++j)
+        if (acn[j] != 0.0) gnorm = fmax(gnorm, fabs(g[j] / fnorm) / acn[j]);
+    }
+    if (gnorm <= 0.0) return 4;  // gtol = 0
+#pragma unroll
+    for (int j = 0; j < N; ++j) D[j] = fmax(D[j], acn[j]);
+    double ratio = 0.0;
+    do {
+      lm_par<N>(A, g, D, delta, par, p);
+#pragma unroll
+      for (int j = 0; j < N; ++j) xt[j] = x[j] + p[j];
+      const double pnorm = dnorm<N>(D, p);
+      if (iter == 1) delta = fmin(delta, pnorm);
+      const double fnorm1 = sqrt(2.0 * cost_at<M>(a, y, xt));
+      nfev += 1;
+      double actred = -1.0;
+      if (0.1 * fnorm1 < fnorm) actred = 1.0 - (fnorm1 / fnorm) * (fnorm1 / fnorm);
+      double jp2 = 0.0;  // ||J p||^2 = p^T A p
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        double row = 0.0;
+#pragma unroll
+        for (int c = 0; c < N; ++c) row += (c >= i ? A[i * N + c] : A[c * N + i]) * p[c];
+        jp2 += p[i] * row;
+      }
+      const double t1 = sqrt(fmax(jp2, 0.0)) / fnorm;
+      const double t2 = sqrt(par) * pnorm / fnorm;
+      const double prered = t1 * t1 + t2 * t2 / 0.5;
+      const double dirder = -(t1 * t1 + t2 * t2);
+      ratio = (prered != 0.0) ? actred / prered : 0.0;
+      if (!isfinite(fnorm1)) ratio = 0.0;
+      if (ratio <= 0.25) {
+        double temp = (actred >= 0.0) ? 0.5 : 0.5 * dirder / (dirder + 0.5 * actred);
+        if (0.1 * fnorm1 >= fnorm || temp < 0.1 || !isfinite(fnorm1)) temp = 0.1;
+        delta = temp * fmin(delta, pnorm / 0.1);
+        par = par / temp;
+      } else if (par == 0.0 || ratio >= 0.75) {
+        delta = pnorm / 0.5;
+        par = 0.5 * par;
+      }
+      if (ratio >= 1e-4) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) x[j] = xt[j];
+        fnorm = fnorm1;
+        xnorm = dnorm<N>(D, x);
+      }
+      int info = 0;
+      if (fabs(actred) <= ftol && prered <= ftol && 0.5 * ratio <= 1.0) info = 1;
+      if (delta <= xtol * xnorm) info = (info == 1) ? 3 : 2;
+      if (info) return info;
+      if (nfev >= maxfev) return 5;
+      if (fabs(actred) <= epsmch && prered <= epsmch && 0.5 * ratio <= 1.0) return 6;
+      if (delta <= epsmch * xnorm) return 7;
+      if (gnorm <= epsmch) return 8;
+    } while (ratio < 1e-4);
+  }
 }
 
 template <int M>
@@ -302,7 +415,8 @@ __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long n
       p[0] = y[0];
       p[1] = a.lam_phys;
     }
-    bool good = finite && a.T >= N && lm_fit<M>(a, y, p);
+    const int info = (finite && a.T >= N) ? lm_fit<M>(a, y, p, a.max_fev) : -1;
+    const bool good = info >= 1 && info <= 4;  // curve_fit raises for any other outcome
     if (!good) {
       if (M == M_MONO_LAMBDA) {  // fallback [0, lam_phys] (curve_fitting.py:58-59)
         p[0] = 0.0;
@@ -339,7 +453,7 @@ __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long n
 using namespace pvd;
 
 extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* weights, int n_times,
-                                  const double* p0, double lam_phys, double auc_limit, int max_iter, int flags,
+                                  const double* p0, double lam_phys, double auc_limit, int max_fev, int flags,
                                   const float* acts_d, long long n_vox, double* params_d, double* auc_d,
                                   unsigned char* ok_d, pvd_stream stream) {
   if (!times || !acts_d || !params_d || !auc_d) return set_error(PVD_ERR_ARG, "pvd_tac_fit: null argument");
@@ -347,7 +461,7 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
   if (n_vox < 0) return set_error(PVD_ERR_ARG, "pvd_tac_fit: negative voxel count");
   if (model < 0 || model > M_LM_TRI) return set_error(PVD_ERR_ARG, "pvd_tac_fit: unknown model");
   if (model != M_MONO_LAMBDA && !p0) return set_error(PVD_ERR_ARG, "pvd_tac_fit: p0 required for this model");
-  if (max_iter < 1) return set_error(PVD_ERR_ARG, "pvd_tac_fit: max_iter must be >= 1");
+  if (max_fev < 1) return set_error(PVD_ERR_ARG, "pvd_tac_fit: max_fev must be >= 1");
   if (n_vox == 0) return PVD_OK;
   FitArgs a;
   a.T = n_times;
@@ -358,7 +472,7 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
   for (int i = 0; i < 5; ++i) a.p0[i] = p0 ? p0[i] : 0.0;
   a.lam_phys = lam_phys;
   a.auc_limit = auc_limit;
-  a.max_iter = max_iter;
+  a.max_fev = max_fev;
   a.force_zero_at_t0 = (flags & PVD_FIT_FORCE_ZERO_AT_T0) ? 1 : 0;
   a.p0_from_data = (model == M_MONO_LAMBDA && !(flags & PVD_FIT_P0_GIVEN)) ? 1 : 0;
   cudaStream_t st = (cudaStream_t)stream;

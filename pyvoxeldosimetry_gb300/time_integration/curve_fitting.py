@@ -24,7 +24,7 @@ MODEL_IDS = {"f2": 1, "f3": 2, "f3a": 3, "f4a": 4, "f4b": 5, "f4c": 6,
              "mono-exponential": 7, "bi-exponential": 8, "tri-exponential": 9}
 NUKFIT = ["f2", "f3", "f3a", "f4a", "f4b", "f4c"]
 LMFIT = ["mono-exponential", "bi-exponential", "tri-exponential"]
-MONO_MAXFEV_ITERS = 200      # curve_fit default maxfev 200*(n+1) evaluations, n+1 per LM iteration
+MONO_MAXFEV = 200 * (2 + 1)  # curve_fit's default maxfev for lmdif with n = 2 parameters
 ADVANCED_MAXFEV = 10000      # curve_fitting.py:206
 
 
@@ -36,7 +36,7 @@ def _p0_table(half_life: float) -> dict:
             "tri-exponential": [1.0, half_life, 0.5, half_life / 2, half_life]}
 
 
-def _run_fit(model_id, n_par, times, weights, p0, lam_phys, auc_limit, max_iter, flags, activities):
+def _run_fit(model_id, n_par, times, weights, p0, lam_phys, auc_limit, max_fev, flags, activities):
     acts = activities if not isinstance(activities, (list, tuple)) else None
     if acts is None:
         kinds = {_io.kind_of(a) for a in activities}
@@ -64,7 +64,7 @@ def _run_fit(model_id, n_par, times, weights, p0, lam_phys, auc_limit, max_iter,
         t = (C.c_double * n_t)(*[float(x) for x in times])
         w = (C.c_double * n_t)(*[float(x) for x in weights]) if weights is not None else None
         p = (C.c_double * 5)(*(list(p0) + [0.0] * (5 - len(p0)))) if p0 is not None else None
-        N.check(lib.pvd_tac_fit(model_id, t, w, n_t, p, float(lam_phys), float(auc_limit), int(max_iter), flags,
+        N.check(lib.pvd_tac_fit(model_id, t, w, n_t, p, float(lam_phys), float(auc_limit), int(max_fev), flags,
                                 a.data_ptr(), nvox, params.data_ptr(), auc.data_ptr(), ok.data_ptr(),
                                 _stream_handle(None)))
         params = params.reshape((n_par, *shape))
@@ -87,7 +87,7 @@ class TimeCurveFitting:
         accumulated = A0/lam (1 - exp(-lam * limit)), limit = 100 T1/2 by default)."""
         limit = 100 * self.half_life if integration_limit is None else integration_limit
         params, auc, ok = _run_fit(0, 2, times, weight_factors, None, self.decay_constant, limit,
-                                   MONO_MAXFEV_ITERS, 0, activities)
+                                   MONO_MAXFEV, 0, activities)
         return (params, auc, ok) if return_success else (params, auc)
 
     def _calculate_accumulated_dose(self, fitted_params, integration_limit: float = None):
@@ -119,7 +119,7 @@ class TimeCurveFitting:
         n_par = len(p0)
         flags = 2 | (1 if force_zero_at_t0 else 0)
         params, auc, ok = _run_fit(MODEL_IDS[model_name], n_par, times, weight_factors, p0, lam_phys, 0.0,
-                                   ADVANCED_MAXFEV // (n_par + 1), flags, activities)
+                                   ADVANCED_MAXFEV, flags, activities)
         if return_fit_params:
             return params, auc, {"model": model, "model_name": model_name, "success": ok}
         return params, auc
