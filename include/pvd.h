@@ -121,6 +121,18 @@ pvd_status pvd_plan_set_kernel(pvd_plan* plan, int slot, const double* kernel_ho
 pvd_status pvd_conv_execute(pvd_plan* plan, const float* activity_d, const float* density_d,
                             float* dose_d, float out_scale, pvd_stream stream);
 
+/* pvd_conv_execute with HOST buffers: activity_h / density_h (nullable) /
+ * dose_h are host float32 arrays of the sizes above.  The plan stages them in
+ * device buffers it owns and pipelines the copies with the passes: the
+ * activity goes up in z chunks that each release their share of the forward
+ * passes, the density goes up during the z pass, and each slot's dose comes
+ * back while the next slot computes.  Returns once queued; the copies back
+ * are complete when `stream` is (cudaStreamSynchronize).  Page-locked host
+ * memory makes the copies asynchronous; pageable memory works but copies
+ * synchronously. */
+pvd_status pvd_conv_execute_host(pvd_plan* plan, const float* activity_h, const float* density_h,
+                                 float* dose_h, float out_scale, pvd_stream stream);
+
 /* As pvd_conv_execute with activity = sum_t weights[t] * activity_d[t]
  * (t < n_act <= PVD_MAX_TIMEPOINTS), the weighted sum fused into the first
  * pass (trapezoid time integration without an extra pass over the volume). */

@@ -135,6 +135,44 @@ class ConvPlan:
         N.check(st)
         return out
 
+    def execute_host(self, activity, density=None, out=None, out_scale: float = 1.0, stream=None):
+        """Dose from HOST arrays (numpy or CPU tensors) through the plan's pipelined
+        host path (pvd_conv_execute_host): uploads, passes and downloads overlap.
+
+        Returns ``out`` (a CPU float32 tensor of shape (n_kernels, *shape), page-locked
+        when allocated here) after the copies back have completed.
+        """
+        keep = []
+
+        def host_ptr(x, what):
+            if isinstance(x, torch.Tensor):
+                if x.device.type != "cpu" or x.dtype != torch.float32 or not x.is_contiguous():
+                    raise TypeError(f"{what} must be a contiguous float32 CPU tensor")
+                if tuple(x.shape) != self.shape:
+                    raise ValueError(f"{what} has shape {tuple(x.shape)}, plan expects {self.shape}")
+                keep.append(x)
+                return x.data_ptr()
+            a = np.ascontiguousarray(x, dtype=np.float32)
+            if a.shape != self.shape:
+                raise ValueError(f"{what} has shape {a.shape}, plan expects {self.shape}")
+            keep.append(a)
+            return a.ctypes.data
+
+        ap = host_ptr(activity, "activity")
+        rp = host_ptr(density, "density") if density is not None else None
+        if out is None:
+            out = torch.empty((self.n_kernels, *self.shape), dtype=torch.float32, pin_memory=True)
+        elif not (isinstance(out, torch.Tensor) and out.device.type == "cpu" and out.dtype == torch.float32
+                  and out.is_contiguous() and tuple(out.shape) == (self.n_kernels, *self.shape)):
+            raise ValueError("out must be a contiguous float32 CPU tensor of shape (n_kernels, *shape)")
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device)
+        with torch.cuda.device(self.device):
+            N.check(self._lib.pvd_conv_execute_host(self._h, ap, rp, out.data_ptr(), float(out_scale),
+                                                    int(stream.cuda_stream)))
+            stream.synchronize()
+        return out
+
     def close(self) -> None:
         h = getattr(self, "_h", None)
         if h is not None and h.value:

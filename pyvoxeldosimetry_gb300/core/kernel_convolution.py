@@ -139,6 +139,8 @@ class KernelConvolutionCalculator(DosimetryCalculator):
             if any(tuple(a.shape) != shape for a in acts):
                 raise ValueError("All activity maps must have the same dimensions")
             plan = self._plan_for(shape, voxel_size, device)
+            if weights is None and kind != _io.CUDA_TENSOR and _io.kind_of(density) != _io.CUDA_TENSOR:
+                return self._run_host(plan, acts[0], density, out_scale, out, kind, shape)
             dev_acts = [_io.to_device(a, device, "activity") for a in acts]
             rho = None
             if density is not None:
@@ -150,6 +152,22 @@ class KernelConvolutionCalculator(DosimetryCalculator):
             if isinstance(self.radionuclide, str):
                 res = res[0]
             return _io.from_device(res, kind, out)
+
+    def _run_host(self, plan, activity, density, out_scale, out, kind, shape):
+        """Host arrays in and out: the plan's pipelined copy/compute path."""
+        if density is not None and tuple(density.shape) != shape:
+            raise ValueError("density map must have the activity map's shape")
+        single = isinstance(self.radionuclide, str)
+        dst = None
+        if out is not None:
+            t = torch.from_numpy(out) if isinstance(out, np.ndarray) else out
+            dst = t.view(1, *shape) if single else t
+        res = plan.execute_host(activity, density, out=dst, out_scale=out_scale)
+        if out is not None:
+            return out
+        if single:
+            res = res[0]
+        return res.numpy() if kind == _io.NUMPY else res
 
     def calculate_dose_rate(self, activity_map, voxel_size: Tuple[float, float, float], density=None, out=None):
         """Dose rate (Gy/s) of an activity map (Bq per voxel).

@@ -40,6 +40,7 @@ constexpr int TXP = TX + 1;   // padded shared-memory row stride (complex)
 constexpr int NT = 256;       // threads per CTA
 constexpr int NL = NT / TX;   // lanes per transform
 constexpr int MAX_STAGES = 16;
+constexpr int PVD_HOST_CHUNKS = 4;  // activity upload chunks overlapped with the forward passes
 
 struct FftLen {
   int L;
@@ -442,6 +443,14 @@ struct pvd_plan {
   std::vector<void*> allocs;
   // per-pass event timing (instrumentation, off by default)
   int prof = 0;
+  // host-buffer execution (pvd_conv_execute_host): device staging and copy streams
+  float* io_act = nullptr;
+  float* io_rho = nullptr;
+  float* io_dose = nullptr;
+  cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_rho = nullptr, ev_done = nullptr;
+  cudaEvent_t ev_act[PVD_HOST_CHUNKS] = {};
+  cudaEvent_t ev_dose[PVD_MAX_KERNELS] = {};
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   struct Rec { int kind; cudaEvent_t a, b; };
@@ -466,6 +475,14 @@ pvd_status plan_alloc(pvd_plan* p, size_t bytes, void** out) {
 void plan_free(pvd_plan* p) {
   for (void* a : p->allocs) cudaFree(a);
   p->allocs.clear();
+  if (p->s_h2d) cudaStreamDestroy(p->s_h2d);
+  if (p->s_d2h) cudaStreamDestroy(p->s_d2h);
+  for (cudaEvent_t e : {p->ev_start, p->ev_rho, p->ev_done})
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->ev_act)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->ev_dose)
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
   p->ev_pool.clear();
 }
@@ -748,8 +765,15 @@ extern "C" pvd_status pvd_plan_set_kernel(pvd_plan* p, int slot, const double* k
   return st;
 }
 
+// Host buffers of one pvd_conv_execute_host call (device staging lives in the plan).
+struct HostIO {
+  const float* act;
+  const float* rho;
+  float* dose;
+};
+
 static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float* dose, float out_scale,
-                           pvd_stream stream) {
+                           pvd_stream stream, const HostIO* hio = nullptr) {
   for (int s = 0; s < p->nk; ++s)
     if (!p->spec_set[s]) return set_error(PVD_ERR_STATE, "pvd_conv_execute: kernel slot " + std::to_string(s) + " not set");
   if (!dose) return set_error(PVD_ERR_ARG, "pvd_conv_execute: null dose pointer");
@@ -758,27 +782,40 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
   const int N0 = p->N[0], N1 = p->N[1], N2 = p->N[2];
   const int nrows = N0 * N1;
   const long long vox = (long long)nrows * N2;
-  const int xblocks = (nrows + 2 * TX - 1) / (2 * TX);
   const int ctiles = p->HS / TX;
 
   const FastLen* fx = p->fl[2];
   const FastLen* fy = p->fl[1];
   const FastLen* fz = p->fl[0];
-  {
-    PassTimer t(p, 0, st);
-    if (fx)
-      fx->x_fwd<<<xblocks, fx->threads, fx->smem_row, st>>>(in, p->buf1, nrows, N2, p->HS, p->tw[2]);
-    else
-      k_x_fwd<<<xblocks, NT, p->smem_x, st>>>(in, p->buf1, nrows, N2, p->HS, p->f[2], p->tw[2]);
-    PVD_LAUNCH_CHECK("x_fwd");
-  }
-  {
-    PassTimer t(p, 1, st);
-    if (fy)
-      fy->y_fwd<<<dim3(ctiles, N0), fy->threads, fy->smem_col, st>>>(p->buf1, p->buf2, N1, p->P[1], p->HS, p->tw[1]);
-    else
-      k_y<false><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf1, p->buf2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
-    PVD_LAUNCH_CHECK("y_fwd");
+  // forward x and y passes, in z chunks when the activity arrives from the host
+  // in pieces (each chunk waits for its own upload)
+  const int nchunks = hio ? std::min(PVD_HOST_CHUNKS, N0) : 1;
+  for (int c = 0; c < nchunks; ++c) {
+    const int z0 = (int)((long long)N0 * c / nchunks), z1 = (int)((long long)N0 * (c + 1) / nchunks);
+    if (z1 <= z0) continue;
+    if (hio) PVD_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_act[c], 0));
+    ActIn ic = in;
+    for (int t = 0; t < ic.n; ++t) ic.p[t] = in.p[t] + (long long)z0 * N1 * N2;
+    const int rows = (z1 - z0) * N1;
+    const int xb = (rows + 2 * TX - 1) / (2 * TX);
+    float2* b1 = p->buf1 + (long long)z0 * N1 * p->HS;
+    float2* b2 = p->buf2 + (long long)z0 * p->P[1] * p->HS;
+    {
+      PassTimer t(p, 0, st);
+      if (fx)
+        fx->x_fwd<<<xb, fx->threads, fx->smem_row, st>>>(ic, b1, rows, N2, p->HS, p->tw[2]);
+      else
+        k_x_fwd<<<xb, NT, p->smem_x, st>>>(ic, b1, rows, N2, p->HS, p->f[2], p->tw[2]);
+      PVD_LAUNCH_CHECK("x_fwd");
+    }
+    {
+      PassTimer t(p, 1, st);
+      if (fy)
+        fy->y_fwd<<<dim3(ctiles, z1 - z0), fy->threads, fy->smem_col, st>>>(b1, b2, N1, p->P[1], p->HS, p->tw[1]);
+      else
+        k_y<false><<<dim3(ctiles, z1 - z0), NT, p->smem_y, st>>>(b1, b2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
+      PVD_LAUNCH_CHECK("y_fwd");
+    }
   }
   // z pass: the fast kernel takes up to FZ_SLOTS kernel slots per launch (each
   // launch reads the forward data again); the generic one takes all of them.
@@ -806,7 +843,9 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
       k_z<<<dim3(ctiles, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
     PVD_LAUNCH_CHECK("z");
   }
+  const int xblocks = (nrows + 2 * TX - 1) / (2 * TX);
   for (int s = 0; s < p->nk; ++s) {
+    if (hio && s == 0 && hio->rho) PVD_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_rho, 0));
     {
       PassTimer t(p, 3, st);
       if (fy)
@@ -827,6 +866,16 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
                                                p->tw[2]);
       PVD_LAUNCH_CHECK("x_inv");
     }
+    if (hio) {  // this slot's dose goes back while the next slot computes
+      PVD_CUDA_TRY(cudaEventRecord(p->ev_dose[s], st));
+      PVD_CUDA_TRY(cudaStreamWaitEvent(p->s_d2h, p->ev_dose[s], 0));
+      PVD_CUDA_TRY(cudaMemcpyAsync(hio->dose + s * vox, dose + s * vox, sizeof(float) * vox, cudaMemcpyDeviceToHost,
+                                   p->s_d2h));
+    }
+  }
+  if (hio) {  // the caller's stream completes only after the last copy back
+    PVD_CUDA_TRY(cudaEventRecord(p->ev_done, p->s_d2h));
+    PVD_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_done, 0));
   }
   return PVD_OK;
 }
@@ -840,6 +889,62 @@ extern "C" pvd_status pvd_conv_execute(pvd_plan* p, const float* act, const floa
   in.p[0] = act;
   in.w[0] = 1.0f;
   return conv_run(p, in, rho, dose, out_scale, stream);
+}
+
+extern "C" pvd_status pvd_conv_execute_host(pvd_plan* p, const float* act_h, const float* rho_h, float* dose_h,
+                                            float out_scale, pvd_stream stream) {
+  if (!p || !act_h || !dose_h) return set_error(PVD_ERR_ARG, "pvd_conv_execute_host: null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int N0 = p->N[0], N1 = p->N[1], N2 = p->N[2];
+  const long long vox = (long long)N0 * N1 * N2;
+  const size_t vb = sizeof(float) * (size_t)vox;
+  // lazily created staging buffers, streams and events (kept for later calls)
+  void* ptr = nullptr;
+  pvd_status as = PVD_OK;
+  if (!p->io_act) {
+    if ((as = plan_alloc(p, vb, &ptr)) != PVD_OK) return as;
+    p->io_act = (float*)ptr;
+  }
+  if (rho_h && !p->io_rho) {
+    if ((as = plan_alloc(p, vb, &ptr)) != PVD_OK) return as;
+    p->io_rho = (float*)ptr;
+  }
+  if (!p->io_dose) {
+    if ((as = plan_alloc(p, vb * p->nk, &ptr)) != PVD_OK) return as;
+    p->io_dose = (float*)ptr;
+  }
+  if (!p->s_h2d) {
+    PVD_CUDA_TRY(cudaStreamCreateWithFlags(&p->s_h2d, cudaStreamNonBlocking));
+    PVD_CUDA_TRY(cudaStreamCreateWithFlags(&p->s_d2h, cudaStreamNonBlocking));
+    PVD_CUDA_TRY(cudaEventCreateWithFlags(&p->ev_start, cudaEventDisableTiming));
+    PVD_CUDA_TRY(cudaEventCreateWithFlags(&p->ev_rho, cudaEventDisableTiming));
+    PVD_CUDA_TRY(cudaEventCreateWithFlags(&p->ev_done, cudaEventDisableTiming));
+    for (auto& e : p->ev_act) PVD_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& e : p->ev_dose) PVD_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  // uploads start after everything already queued on the caller's stream (which
+  // may still read the staging buffers of a previous call)
+  PVD_CUDA_TRY(cudaEventRecord(p->ev_start, st));
+  PVD_CUDA_TRY(cudaStreamWaitEvent(p->s_h2d, p->ev_start, 0));
+  const int nchunks = std::min(PVD_HOST_CHUNKS, N0);
+  for (int c = 0; c < nchunks; ++c) {
+    const long long z0 = (long long)N0 * c / nchunks, z1 = (long long)N0 * (c + 1) / nchunks;
+    const long long off = z0 * N1 * N2, n = (z1 - z0) * N1 * N2;
+    if (n > 0)
+      PVD_CUDA_TRY(cudaMemcpyAsync(p->io_act + off, act_h + off, sizeof(float) * n, cudaMemcpyHostToDevice, p->s_h2d));
+    PVD_CUDA_TRY(cudaEventRecord(p->ev_act[c], p->s_h2d));
+  }
+  if (rho_h) {
+    PVD_CUDA_TRY(cudaMemcpyAsync(p->io_rho, rho_h, vb, cudaMemcpyHostToDevice, p->s_h2d));
+    PVD_CUDA_TRY(cudaEventRecord(p->ev_rho, p->s_h2d));
+  }
+  ActIn in;
+  std::memset(&in, 0, sizeof(in));
+  in.n = 1;
+  in.p[0] = p->io_act;
+  in.w[0] = 1.0f;
+  HostIO hio{act_h, rho_h, dose_h};
+  return conv_run(p, in, rho_h ? p->io_rho : nullptr, p->io_dose, out_scale, stream, &hio);
 }
 
 extern "C" pvd_status pvd_conv_execute_weighted(pvd_plan* p, const float* const* act, const float* w, int n_act,

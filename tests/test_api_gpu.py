@@ -117,3 +117,30 @@ def test_api_errors_match_reference_conventions():
     calc.calculator.kernel = np.ones((3, 3, 3))
     with pytest.raises(ValueError, match="kernel_resolution"):
         calc.calculator.calculate_dose_rate(a, (2.0, 2.0, 2.0))
+
+
+def test_host_buffer_path_is_identical_to_device_path():
+    """numpy / pinned-CPU-tensor inputs take the pipelined host path
+    (pvd_conv_execute_host); it runs the same kernels, so the dose is bitwise equal
+    to the device-resident path, for one and for several nuclides."""
+    from pyvoxeldosimetry_gb300 import KernelConvolutionCalculator
+    rng = np.random.default_rng(13)
+    shape = (37, 30, 41)
+    a = rng.random(shape).astype(np.float32) * 1e4
+    rho = rng.uniform(0.2, 1.9, shape).astype(np.float32)
+    for nucs in ("Y90", ["Y90", "Lu177", "I131"]):
+        calc = KernelConvolutionCalculator(nucs, "water", config={"kernel_size": {"Y90": 21, "Lu177": 9, "I131": 11}})
+        dev = calc.calculate_dose_rate(torch.from_numpy(a).cuda(), (1.5,) * 3, density=torch.from_numpy(rho).cuda())
+        dev = dev.cpu().numpy()
+        host_np = calc.calculate_dose_rate(a, (1.5,) * 3, density=rho)
+        assert isinstance(host_np, np.ndarray) and host_np.shape == dev.shape
+        np.testing.assert_array_equal(host_np, dev)
+        at, rt = torch.from_numpy(a).pin_memory(), torch.from_numpy(rho).pin_memory()
+        out = torch.empty(dev.shape, dtype=torch.float32).pin_memory()
+        for _ in range(3):  # repeated calls reuse the plan's staging buffers and streams
+            res = calc.calculate_dose_rate(at, (1.5,) * 3, density=rt, out=out)
+            assert res is out
+            np.testing.assert_array_equal(out.numpy(), dev)
+        # without density
+        np.testing.assert_array_equal(calc.calculate_dose_rate(a, (1.5,) * 3),
+                                      calc.calculate_dose_rate(torch.from_numpy(a).cuda(), (1.5,) * 3).cpu().numpy())
