@@ -142,6 +142,33 @@ pvd_status pvd_conv_execute_weighted(pvd_plan* plan, const float* const* activit
 
 pvd_status pvd_plan_destroy(pvd_plan* plan);
 
+/* Allocation-free convolution.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory themselves or let a library
+ * do it (a host framework that owns the device allocator and its budget, a
+ * plugin that must not call cudaMalloc/cudaFree because they synchronise the
+ * device, code that must not grow the process's footprint per call).  It runs
+ * the pvd_conv_execute pipeline (LINEAR mode, one kernel, density optional)
+ * with every temporary (twiddles, kernel staging, spectrum, spectral work
+ * buffers) placed in one static device array of PVD_STATIC_SCRATCH_BYTES that
+ * each GPU loading this library holds until the process exits.  The caller
+ * passes the inputs (device activity/density, host FP64 kernel) and the output
+ * (device dose); nothing is allocated.  Volumes whose scratch would exceed the
+ * array (about 128^3 with a 15^3 kernel fits) are rejected with
+ * PVD_ERR_UNSUPPORTED and a message giving the bytes needed.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current) and caches it; make that
+ * first call before any stream capture.  Every call uses the same array: calls
+ * that can overlap on the GPU (other streams, other host threads) race and
+ * must be serialised by the caller.  The kernel upload is a plain host-to-device
+ * copy on `stream`. */
+#define PVD_STATIC_SCRATCH_BYTES (64ull << 20)
+#define PVD_STATIC_MAX_DEVICES 64
+pvd_status pvd_conv_execute_static(const float* activity_d, const float* density_d, float* dose_d,
+                                   int n0, int n1, int n2, const double* kernel_h, int k0, int k1, int k2,
+                                   double scale, int flags, float out_scale, pvd_stream stream);
+
 /* FFT lengths that have register-resident (four-step) pass kernels; LINEAR
  * plans pad to one of them when it costs <= 25 % over the minimum.  Writes up
  * to `cap` lengths (ascending) and returns how many exist. */

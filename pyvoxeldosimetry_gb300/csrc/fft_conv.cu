@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -995,4 +996,206 @@ extern "C" pvd_status pvd_plan_destroy(pvd_plan* p) {
   plan_free(p);
   delete p;
   return PVD_OK;
+}
+
+// ===========================================================================
+// Allocation-free convolution (no counterpart in the reference).
+//
+// Some callers cannot allocate device memory: code that runs under a memory
+// budget enforced by a host framework that owns the allocator, plugins that
+// must not call cudaMalloc/cudaFree (they synchronise the device and would
+// stall the host application's streams), or callers inside stream capture.
+// pvd_conv_execute_static runs the same five-pass pipeline as a plan, with all
+// of its scratch (twiddles, kernel staging, spectrum, the two spectral work
+// buffers) carved out of one file-scope device array of PVD_STATIC_SCRATCH_BYTES.
+// The host code below never uses the array's name as an address: on the first
+// call on a device (with that device current) it asks the runtime for the
+// array's device address with cudaGetSymbolAddress and caches it per device.
+// ===========================================================================
+
+namespace {
+
+__device__ __align__(256) unsigned char g_conv_scratch[PVD_STATIC_SCRATCH_BYTES];
+
+std::mutex g_scratch_mu;
+void* g_scratch_addr[PVD_STATIC_MAX_DEVICES] = {};
+
+// Device address of g_conv_scratch on the current device (looked up once per device).
+pvd_status static_scratch_address(void** out) {
+  int dev = 0;
+  PVD_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= PVD_STATIC_MAX_DEVICES)
+    return set_error(PVD_ERR_UNSUPPORTED, "pvd_conv_execute_static: device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* addr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&addr, g_conv_scratch);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_conv_scratch)");
+    g_scratch_addr[dev] = addr;
+  }
+  *out = g_scratch_addr[dev];
+  return PVD_OK;
+}
+
+// twiddles exp(-2 pi i n / L) computed on the device (no host staging buffer)
+__global__ void k_twiddle(float2* __restrict__ tw, int L) {
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < L; n += gridDim.x * blockDim.x) {
+    float s, c;
+    sincospif(-2.0f * (float)n / (float)L, &s, &c);
+    tw[n] = make_float2(c, s);
+  }
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" pvd_status pvd_conv_execute_static(const float* activity_d, const float* density_d, float* dose_d,
+                                              int n0, int n1, int n2, const double* kernel_h, int k0, int k1,
+                                              int k2, double scale, int flags, float out_scale, pvd_stream stream) {
+  if (!activity_d || !dose_d || !kernel_h) return set_error(PVD_ERR_ARG, "pvd_conv_execute_static: null argument");
+  if (flags & ~PVD_KERNEL_NORMALIZE) return set_error(PVD_ERR_ARG, "pvd_conv_execute_static: unknown flags");
+  const int N[3] = {n0, n1, n2}, K[3] = {k0, k1, k2};
+  for (int i = 0; i < 3; ++i) {
+    if (N[i] < 1 || N[i] > 4096) return set_error(PVD_ERR_ARG, "pvd_conv_execute_static: volume dims must be in [1, 4096]");
+    if (K[i] < 1 || K[i] > 1024) return set_error(PVD_ERR_ARG, "pvd_conv_execute_static: kernel dims must be in [1, 1024]");
+  }
+  if (!std::isfinite(scale) || !std::isfinite(out_scale))
+    return set_error(PVD_ERR_NUMERIC, "pvd_conv_execute_static: non-finite scale");
+  const long long nk = (long long)k0 * k1 * k2;
+  for (long long i = 0; i < nk; ++i)
+    if (!std::isfinite(kernel_h[i])) return set_error(PVD_ERR_NUMERIC, "pvd_conv_execute_static: non-finite kernel value");
+
+  // plan on the stack: same length choice and pass kernels as pvd_plan_create (LINEAR, one slot)
+  pvd_plan p;
+  p.mode = PVD_MODE_LINEAR;
+  p.nk = 1;
+  for (int i = 0; i < 3; ++i) {
+    p.N[i] = N[i];
+    p.kmax[i] = K[i];
+    const int need = N[i] + K[i] - 1;
+    const int lf = fast_len_at_least(need), ls = next_smooth7(need);
+    const int L = (lf && (lf == ls || 4 * lf <= 5 * need)) ? lf : ls;
+    if (!factorize(L, &p.f[i])) return set_error(PVD_ERR_UNSUPPORTED, "pvd_conv_execute_static: FFT length not 7-smooth");
+    p.P[i] = L;
+    p.fl[i] = fast_len(L);
+  }
+  p.H = p.P[2] / 2 + 1;
+  p.HS = (p.H + TX - 1) / TX * TX;
+  p.smem_x = smem_bytes(p.P[2], 2);
+  p.smem_y = smem_bytes(p.P[1], 2);
+  p.smem_z = smem_bytes(p.P[0], 2);
+
+  // real-even spectrum for kernels that are even along every axis (as pvd_plan_set_kernel)
+  bool sym = true;
+  for (int i = 0; i < 3; ++i)
+    if (K[i] % 2 == 0) sym = false;
+  for (long long i = 0; sym && i < nk; ++i) {
+    const int a = (int)(i / ((long long)k1 * k2)), b = (int)((i / k2) % k1), c = (int)(i % k2);
+    const long long jz = ((long long)(k0 - 1 - a) * k1 + b) * k2 + c;
+    const long long jy = ((long long)a * k1 + (k1 - 1 - b)) * k2 + c;
+    const long long jx = ((long long)a * k1 + b) * k2 + (k2 - 1 - c);
+    if (kernel_h[i] != kernel_h[jz] || kernel_h[i] != kernel_h[jy] || kernel_h[i] != kernel_h[jx]) sym = false;
+  }
+  const int smode = sym ? SPEC_REAL_EVEN : SPEC_COMPLEX;
+
+  // scratch layout (256-byte aligned regions); T1 / T2 of the spectrum build
+  // share the two spectral work buffers, which the pipeline fills afterwards
+  const size_t b_tw0 = sizeof(float2) * p.P[0], b_tw1 = sizeof(float2) * p.P[1], b_tw2 = sizeof(float2) * p.P[2];
+  const size_t b_spec = sym ? sizeof(float) * (size_t)(p.P[0] / 2 + 1) * (p.P[1] / 2 + 1) * p.HS
+                            : sizeof(float2) * (size_t)p.P[0] * p.P[1] * p.HS;
+  const size_t b_buf1 = std::max(sizeof(float2) * (size_t)n0 * n1 * p.HS, sizeof(float2) * (size_t)k0 * p.P[1] * p.H);
+  const size_t b_buf2 = std::max(sizeof(float2) * (size_t)n0 * p.P[1] * p.HS, sizeof(float2) * (size_t)k0 * k1 * p.H);
+  const size_t b_kd = sizeof(double) * (size_t)nk, b_kf = sizeof(float) * (size_t)nk, b_sum = sizeof(double);
+  size_t off = 0;
+  const size_t o_tw0 = off; off += align256(b_tw0);
+  const size_t o_tw1 = off; off += align256(b_tw1);
+  const size_t o_tw2 = off; off += align256(b_tw2);
+  const size_t o_spec = off; off += align256(b_spec);
+  const size_t o_buf1 = off; off += align256(b_buf1);
+  const size_t o_buf2 = off; off += align256(b_buf2);
+  const size_t o_kd = off; off += align256(b_kd);
+  const size_t o_kf = off; off += align256(b_kf);
+  const size_t o_sum = off; off += align256(b_sum);
+  if (off > PVD_STATIC_SCRATCH_BYTES)
+    return set_error(PVD_ERR_UNSUPPORTED, "pvd_conv_execute_static: this volume/kernel needs " + std::to_string(off) +
+                                              " bytes of scratch, more than the static maximum of " +
+                                              std::to_string((size_t)PVD_STATIC_SCRATCH_BYTES) +
+                                              " bytes; use a plan (pvd_plan_create)");
+  void* base = nullptr;
+  pvd_status st0 = static_scratch_address(&base);
+  if (st0 != PVD_OK) return st0;
+  unsigned char* sb = (unsigned char*)base;
+  p.tw[0] = (float2*)(sb + o_tw0);
+  p.tw[1] = (float2*)(sb + o_tw1);
+  p.tw[2] = (float2*)(sb + o_tw2);
+  p.spec[0] = sb + o_spec;
+  p.spec_mode[0] = smode;
+  p.spec_set[0] = 1;
+  p.buf1 = (float2*)(sb + o_buf1);
+  p.buf2 = (float2*)(sb + o_buf2);
+  p.buf3[0] = p.buf2;
+  double* kd = (double*)(sb + o_kd);
+  float* kf = (float*)(sb + o_kf);
+  double* sumd = (double*)(sb + o_sum);
+
+  int smem_max = 0, cur = 0;
+  PVD_CUDA_TRY(cudaGetDevice(&cur));
+  PVD_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, cur));
+  cudaFuncSetAttribute(k_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute(k_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute(k_y<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute(k_y<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute(k_z, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  for (int i = 0; i < 3; ++i) {
+    const FastLen* f = p.fl[i];
+    if (!f) continue;
+    cudaFuncSetAttribute((const void*)f->x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+    cudaFuncSetAttribute((const void*)f->x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+    cudaFuncSetAttribute((const void*)f->y_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+    cudaFuncSetAttribute((const void*)f->y_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+    cudaFuncSetAttribute((const void*)f->z, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  }
+  const size_t need_x = p.fl[2] ? p.fl[2]->smem_row : p.smem_x;
+  const size_t need_y = p.fl[1] ? p.fl[1]->smem_col : p.smem_y;
+  const size_t need_z = p.fl[0] ? p.fl[0]->smem_z : p.smem_z;
+  if ((int)std::max({need_x, need_y, need_z}) > smem_max)
+    return set_error(PVD_ERR_UNSUPPORTED, "pvd_conv_execute_static: FFT length too large for one shared-memory tile");
+
+  cudaStream_t st = (cudaStream_t)stream;
+  for (int i = 0; i < 3; ++i) {
+    k_twiddle<<<(p.P[i] + 255) / 256, 256, 0, st>>>(p.tw[i], p.P[i]);
+    PVD_LAUNCH_CHECK("k_twiddle");
+  }
+  // kernel spectrum (FP64 normalisation sum on the GPU when asked), into scratch
+  PVD_CUDA_TRY(cudaMemcpyAsync(kd, kernel_h, b_kd, cudaMemcpyHostToDevice, st));
+  const bool norm = (flags & PVD_KERNEL_NORMALIZE) != 0;
+  if (norm) {
+    k_sum_f64<<<1, NT, 0, st>>>(kd, nk, sumd);
+    PVD_LAUNCH_CHECK("k_sum_f64");
+  }
+  const double inv_p = 1.0 / ((double)p.P[0] * p.P[1] * p.P[2]);
+  const int o[3] = {k0 / 2, k1 / 2, k2 / 2};
+  const int Ke[3] = {std::min(k0, p.P[0]), std::min(k1, p.P[1]), std::min(k2, p.P[2])};
+  const int gs = 152 * 8;
+  float2* t1 = p.buf2;
+  float2* t2 = p.buf1;
+  k_scale_to_f32<<<gs, NT, 0, st>>>(kd, nk, norm ? sumd : nullptr, scale * inv_p, kf);
+  PVD_LAUNCH_CHECK("k_scale_to_f32");
+  k_spec_x<<<gs, NT, 0, st>>>(kf, t1, k0, k1, k2, Ke[2], o[2], p.P[2], p.H, p.tw[2]);
+  PVD_LAUNCH_CHECK("k_spec_x");
+  k_spec_y<<<gs, NT, 0, st>>>(t1, t2, k0, k1, Ke[1], o[1], p.P[1], p.H, p.tw[1]);
+  PVD_LAUNCH_CHECK("k_spec_y");
+  k_spec_z<<<gs, NT, 0, st>>>(t2, p.spec[0], smode, Ke[0], o[0], p.P[0], p.P[1], p.H, p.HS, p.tw[0]);
+  PVD_LAUNCH_CHECK("k_spec_z");
+  // the array keeps the previous call's contents: the padding columns [H, HS)
+  // of the first work buffer must start at zero
+  PVD_CUDA_TRY(cudaMemsetAsync(p.buf1, 0, sizeof(float2) * (size_t)n0 * n1 * p.HS, st));
+
+  ActIn in;
+  std::memset(&in, 0, sizeof(in));
+  in.n = 1;
+  in.p[0] = activity_d;
+  in.w[0] = 1.0f;
+  return conv_run(&p, in, density_d, dose_d, out_scale, stream);
 }
