@@ -223,6 +223,68 @@ pvd_status pvd_tac_fit(int model, const double* times, const double* weights, in
                        unsigned char* ok_d, pvd_stream stream);
 
 /* ------------------------------------------------------------------------ */
+/* Monte Carlo transport                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* One thread per decay history: decays sampled in proportion to the activity
+ * (voxel by an integer prefix sum, uniform position inside it), one beta with
+ * probability beta_yield (energy from the inverse-CDF table) and each gamma line
+ * with its yield, isotropic.  Electrons: continuous slowing down along voxel-
+ * bounded steps (<= 1/4 of the residual CSDA range), range table scaled by the
+ * local density, Highland multiple scattering in water.  Photons: Woodcock
+ * tracking with the total mass attenuation table, absorption or Compton
+ * (Klein-Nishina, Kahn's method) with the electron deposited locally.  Energy
+ * is scored in unsigned 64-bit fixed point, 2^-32 MeV per unit, so results are
+ * bit-reproducible for a given seed.  Tables are uniform in energy:
+ * E_i = i * de.  Replaces MonteCarloCalculator (core/monte_carlo.py:10-172). */
+#define PVD_MC_MAX_GAMMA 8
+typedef struct {
+  int n[3];                  /* volume dims (C order) */
+  double voxel_mm[3];        /* voxel size per axis (mm) */
+  const float* beta_icdf;    /* host: beta energy (MeV) at u = i/(n_beta-1) */
+  int n_beta;
+  const float* range;        /* host: electron CSDA range in water (g/cm^2) at E_i */
+  int n_range;
+  float range_de;
+  const float* mu_rho;       /* host: photon total mass attenuation of water (cm^2/g) at E_i */
+  const float* compton_frac; /* host: Compton share of mu_rho at E_i */
+  int n_photon;
+  float photon_de;
+  int n_gamma;
+  float gamma_e[PVD_MC_MAX_GAMMA];      /* MeV */
+  float gamma_yield[PVD_MC_MAX_GAMMA];  /* photons per decay (<= 1) */
+  float beta_yield;          /* betas per decay (<= 1) */
+  float e_cut;               /* MeV: particles below it deposit locally */
+} pvd_mc_desc;
+
+typedef struct {
+  unsigned long long total_weight;  /* sum of the fixed-point source weights */
+  unsigned long long emitted;       /* emitted energy, 2^-32 MeV units */
+  unsigned long long escaped;       /* energy leaving the volume, 2^-32 MeV units */
+  unsigned long long steps;         /* transport steps taken */
+  double activity_bq;               /* activity the histories represent (sum of the map) */
+} pvd_mc_stats;
+
+typedef struct pvd_mc_plan pvd_mc_plan;
+
+/* Copy the tables to the device and allocate the source-sampling workspace. */
+pvd_status pvd_mc_plan_create(const pvd_mc_desc* desc, pvd_mc_plan** out);
+
+/* Run n_histories decays with Philox4x32-10 stream `seed`.
+ *   activity_d : device float32 [n] (Bq per voxel; <= 0 and NaN count as 0)
+ *   density_d  : device float32 [n] g/cc or NULL (water)
+ *   edep_d     : device uint64 [n], zeroed then filled with deposited energy
+ *   dose_rate_d: device float32 [n] or NULL: Gy/s = E / n_histories * activity
+ *                * 1.602176634e-13 J/MeV / voxel mass (0 where density <= 0)
+ *   stats      : host or NULL; when given, the call waits for the stream. */
+pvd_status pvd_mc_run(pvd_mc_plan* plan, const float* activity_d, const float* density_d,
+                      unsigned long long n_histories, unsigned long long seed,
+                      unsigned long long* edep_d, float* dose_rate_d, pvd_mc_stats* stats,
+                      pvd_stream stream);
+
+pvd_status pvd_mc_plan_destroy(pvd_mc_plan* plan);
+
+/* ------------------------------------------------------------------------ */
 /* Misc                                                                       */
 /* ------------------------------------------------------------------------ */
 

@@ -12,6 +12,8 @@ from .core.dosimetry_base import DosimetryCalculator
 from .core.kernel_convolution import KernelConvolutionCalculator
 from .core.activity_sampler import ActivitySampler
 from .core.dose_calculator import DoseCalculator, DoseCalculationResult
+from .core.monte_carlo import MonteCarloCalculator
+from .time_integration.curve_fitting import TimeCurveFitting
 
 __all__ = [
     "DosimetryCalculator",
@@ -19,4 +21,6 @@ __all__ = [
     "ActivitySampler",
     "DoseCalculator",
     "DoseCalculationResult",
+    "MonteCarloCalculator",
+    "TimeCurveFitting",
 ]

@@ -29,6 +29,7 @@ EXPORTED_SYMBOLS = [
     "pvd_conv_execute_host", "pvd_conv_execute_weighted", "pvd_plan_destroy", "pvd_conv_execute_static",
     "pvd_fast_lengths", "pvd_plan_profile", "pvd_plan_pass_times",
     "pvd_weighted_sum", "pvd_tac_fit",
+    "pvd_mc_plan_create", "pvd_mc_run", "pvd_mc_plan_destroy",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
 ]
 
@@ -44,6 +45,20 @@ class PvdError(RuntimeError):
 class ConvDesc(C.Structure):
     _fields_ = [("n", C.c_int * 3), ("kmax", C.c_int * 3), ("mode", C.c_int), ("n_kernels", C.c_int),
                 ("pad", C.c_int * 3), ("flags", C.c_int)]
+
+
+class McDesc(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("voxel_mm", C.c_double * 3),
+                ("beta_icdf", C.c_void_p), ("n_beta", C.c_int),
+                ("range", C.c_void_p), ("n_range", C.c_int), ("range_de", C.c_float),
+                ("mu_rho", C.c_void_p), ("compton_frac", C.c_void_p), ("n_photon", C.c_int), ("photon_de", C.c_float),
+                ("n_gamma", C.c_int), ("gamma_e", C.c_float * 8), ("gamma_yield", C.c_float * 8),
+                ("beta_yield", C.c_float), ("e_cut", C.c_float)]
+
+
+class McStats(C.Structure):
+    _fields_ = [("total_weight", C.c_ulonglong), ("emitted", C.c_ulonglong), ("escaped", C.c_ulonglong),
+                ("steps", C.c_ulonglong), ("activity_bq", C.c_double)]
 
 
 class PlanInfo(C.Structure):
@@ -92,6 +107,9 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_plan_pass_times": (st, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
         "pvd_weighted_sum": (st, [vp, vp, i, C.c_longlong, vp, vp]),
         "pvd_tac_fit": (st, [i, vp, vp, i, vp, d, d, i, i, vp, C.c_longlong, vp, vp, vp, vp]),
+        "pvd_mc_plan_create": (st, [C.POINTER(McDesc), C.POINTER(vp)]),
+        "pvd_mc_run": (st, [vp, vp, vp, C.c_ulonglong, C.c_ulonglong, vp, vp, C.POINTER(McStats), vp]),
+        "pvd_mc_plan_destroy": (st, [vp]),
         "pvd_last_error": (st, [C.c_char_p, C.c_size_t]),
         "pvd_version": (i, []),
         "pvd_launch_count": (C.c_uint64, [i]),
