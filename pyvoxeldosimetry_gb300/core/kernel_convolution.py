@@ -24,7 +24,10 @@ Differences from the reference, each deliberate:
     weighted activity (identical by linearity) with the weighting fused into
     the first FFT pass;
   * results are float32 and come back in the caller's array kind (numpy in ->
-    numpy out, CUDA tensor in -> CUDA tensor out).
+    numpy out, CUDA tensor in -> CUDA tensor out);
+  * the FFT lengths of a new (shape, kernel size) are chosen by timing the
+    candidates once (``pyvoxeldosimetry_gb300.autotune``, cached on disk);
+    ``config['autotune'] = False`` takes the smallest fast length instead.
 """
 from __future__ import annotations
 
@@ -118,7 +121,11 @@ class KernelConvolutionCalculator(DosimetryCalculator):
             self._plan.close()
             self._plan = None
         kmax = tuple(max(k.shape[i] for k, _, _ in specs) for i in range(3))
-        plan = ConvPlan(shape, kmax=kmax, n_kernels=len(specs), mode=self.mode, device=device)
+        pads = None
+        if self.mode == "linear" and self.config.get("autotune", True):
+            from ..autotune import tune
+            pads = tune(shape, kmax, len(specs), device=device)
+        plan = ConvPlan(shape, kmax=kmax, n_kernels=len(specs), mode=self.mode, pad=pads, device=device)
         for slot, (k, s, nm) in enumerate(specs):
             plan.set_kernel(slot, k, scale=s, normalize=nm)
         self._plan, self._plan_key = plan, key

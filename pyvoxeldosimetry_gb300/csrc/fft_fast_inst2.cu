@@ -1,4 +1,4 @@
-// Instantiations of the fast convolution pass kernels, lengths 280, 288, 320, 336, 384, 400.
+// Instantiations of the fast convolution pass kernels, lengths 280, 288, 320, 336, 300, 324, 384.
 #include <vector>
 
 #include "fft_fast.cuh"
@@ -10,8 +10,9 @@ void fast_lens_part2(std::vector<FastLen>& v) {
   v.push_back(make_fast_len<16, 18>());  // 288
   v.push_back(make_fast_len<16, 20>());  // 320
   v.push_back(make_fast_len<16, 21>());  // 336
+  v.push_back(make_fast_len<15, 20>());  // 300
+  v.push_back(make_fast_len<18, 18>());  // 324
   v.push_back(make_fast_len<16, 24>());  // 384
-  v.push_back(make_fast_len<20, 20>());  // 400
 }
 
 }  // namespace pvd

@@ -11,6 +11,7 @@ void fast_lens_part0(std::vector<FastLen>& v);
 void fast_lens_part1(std::vector<FastLen>& v);
 void fast_lens_part2(std::vector<FastLen>& v);
 void fast_lens_part3(std::vector<FastLen>& v);
+void fast_lens_part4(std::vector<FastLen>& v);
 
 static const std::vector<FastLen>& fast_table() {
   static const std::vector<FastLen> t = [] {
@@ -19,6 +20,7 @@ static const std::vector<FastLen>& fast_table() {
     fast_lens_part1(v);
     fast_lens_part2(v);
     fast_lens_part3(v);
+    fast_lens_part4(v);
     std::sort(v.begin(), v.end(), [](const FastLen& a, const FastLen& b) { return a.L < b.L; });
     return v;
   }();

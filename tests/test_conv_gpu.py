@@ -141,8 +141,11 @@ def _fast_lengths():
     return _native.fast_lengths()
 
 
-@pytest.mark.parametrize("L", [64, 72, 80, 96, 112, 128, 144, 160, 192, 224, 240, 256, 280, 288, 320, 336, 384,
-                               400, 448, 512, 560, 576, 640])
+FAST_LENGTHS = [64, 72, 80, 96, 112, 128, 144, 160, 192, 224, 240, 252, 256, 270, 280, 288, 300, 320, 324, 336,
+                360, 384, 400, 448, 480, 512, 560, 576, 640]
+
+
+@pytest.mark.parametrize("L", FAST_LENGTHS)
 def test_every_fast_length_on_every_axis(L):
     """Force FFT length L on all three axes (small volume): exercises the register
     four-step x/y/z pass kernels of that length with a real-even (radial) kernel

@@ -37,7 +37,9 @@ def test_errors_without_gpu_are_status_codes():
 
 
 def test_fast_length_registry():
+    from tests.test_conv_gpu import FAST_LENGTHS
     lens = _native.fast_lengths()
+    assert lens == FAST_LENGTHS  # every registered length is exercised by the GPU tests
     assert lens == sorted(lens) and 280 in lens and 144 in lens
     for L in lens:
         r = L
