@@ -201,6 +201,73 @@ def run_reference(args, wl, rank):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(ms: float, device=None) -> float:
+    """Elapsed time of the slowest rank (the job's time); identity without a process group."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world: int, units_per_rank_step: int, steps: int, max_ms: float) -> float:
+    """Whole-job Gvoxel/s: every rank processes its own replica each step (weak scaling)."""
+    return world * units_per_rank_step * steps / (max_ms / 1e3) / 1e9
+
+
+def measure_mc(device, n_hist=10_000_000, reps=3):
+    """GPU Monte Carlo throughput: Lu-177 (beta + gammas) on a 128^3 CT-like phantom at 3 mm."""
+    import torch
+    from pyvoxeldosimetry_gb300 import phantoms
+    from pyvoxeldosimetry_gb300.core.monte_carlo import McPlan, physics_tables
+    act, rho = phantoms.ct_phantom((128, 128, 128), 3.0, seed=4)
+    a = torch.from_numpy(act).to(device)
+    r = torch.from_numpy(rho).to(device)
+    plan = McPlan(act.shape, (3.0, 3.0, 3.0), physics_tables("Lu177"), device)
+    plan.run(a, r, n_hist // 10, 1, dose=True)
+    ms = []
+    for i in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _, _, st = plan.run(a, r, n_hist, 100 + i, dose=True, stats=False)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    plan.close()
+    t = float(np.median(ms))
+    return {"value": n_hist / (t / 1e3) / 1e6, "unit": "Mhistories/s", "ms_per_run": t, "histories": n_hist,
+            "workload": "Lu-177 beta+gamma, 128^3 CT phantom at 3 mm, dose-rate map included"}
+
+
+def measure_fit(device, shape=(256, 256, 256), reps=2):
+    """Per-voxel FP64 mono-exponential fit (+ AUC) throughput, 4 timepoints of bi-exponential washout."""
+    import torch
+    from pyvoxeldosimetry_gb300.time_integration import TimeCurveFitting
+    times = [1.0, 4.0, 24.0, 96.0]
+    g = torch.Generator(device=device).manual_seed(3)
+    a0 = torch.rand(shape, generator=g, device=device) * 1e4 + 1e2
+    l1 = 0.6931 / (6.0 * (160.0 / 6.0) ** torch.rand(shape, generator=g, device=device))
+    l2 = 0.6931 / (6.0 * (160.0 / 6.0) ** torch.rand(shape, generator=g, device=device))
+    w = 0.2 + 0.6 * torch.rand(shape, generator=g, device=device)
+    acts = torch.stack([a0 * (w * torch.exp(-l1 * t) + (1 - w) * torch.exp(-l2 * t)) for t in times]).contiguous()
+    tf = TimeCurveFitting(64.1)
+    tf.fit_time_activity_curve(times, acts[:, :8, :, :].contiguous())
+    ms = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        tf.fit_time_activity_curve(times, acts)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t = float(np.median(ms))
+    nv = int(np.prod(shape))
+    return {"value": nv / (t / 1e3) / 1e9, "unit": "Gvoxel/s", "ms_per_run": t, "voxels": nv,
+            "workload": "mono-exponential FP64 fit + AUC per voxel, 4 timepoints, 256^3"}
+
+
 def config_dict(name, wl):
     return {"workload": name, "shape": list(wl["shape"]), "voxel_mm": wl["voxel_mm"],
             "kernels": {n: [wl["ksize"][n]] * 3 for n in wl["nuclides"]}, "density_scaled": wl["density"],
@@ -218,6 +285,7 @@ def main():
     ap.add_argument("--workload", default="ct256_y90_lu177_i131", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the MC and fit throughput sub-measurements")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -284,18 +352,14 @@ def main():
         barrier()
     launches = int(lib.pvd_launch_count(0))
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = float(np.sum(step_ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(np.sum(step_ms)), device)
     ms_arr = (ctypes.c_double * 5)()
     cnt_arr = (ctypes.c_int * 5)()
     N.check(lib.pvd_plan_pass_times(plan._h, ms_arr, cnt_arr))
     N.check(lib.pvd_plan_profile(plan._h, 0))
     pass_ms = {PASS_NAMES[i]: float(ms_arr[i]) for i in range(5)}
     pass_n = {PASS_NAMES[i]: int(cnt_arr[i]) for i in range(5)}
-    value = world * nk * vox * args.steps / (total_ms / 1e3) / 1e9
+    value = job_throughput(world, nk * vox, args.steps, total_ms)
 
     # roofline of the dominant pass
     kmax = [max(wl["ksize"][n] for n in wl["nuclides"])] * 3
@@ -342,16 +406,16 @@ def main():
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
         barrier()
-        e2e_ms = float(np.sum([a.elapsed_time(b) for a, b in ev]))
-        if world > 1:
-            t = torch.tensor([e2e_ms], device=device)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_ms = float(t.item())
-        line["e2e"] = {"value": world * nk * vox * args.steps / (e2e_ms / 1e3) / 1e9, "unit": UNIT,
+        e2e_ms = max_over_ranks(float(np.sum([a.elapsed_time(b) for a, b in ev])), device)
+        line["e2e"] = {"value": job_throughput(world, nk * vox, args.steps, e2e_ms), "unit": UNIT,
                        "h2d_bytes_per_step": 4 * vox * (2 if rho is not None else 1),
                        "d2h_bytes_per_step": 4 * vox * nk, "ms_per_step": e2e_ms / args.steps,
                        "wall_ms_per_step": 1e3 * wall / args.steps,
                        "api": "KernelConvolutionCalculator.calculate_dose_rate(pinned CPU tensors)"}
+
+    if not args.no_extras:
+        line["mc"] = measure_mc(device)
+        line["tac_fit"] = measure_fit(device)
 
     if rank == 0 and not args.no_cpu_baseline:
         ks = reference_kernels(wl)
