@@ -70,6 +70,11 @@ typedef enum {
  *                      (output shifted by k//2 relative to LINEAR). */
 enum { PVD_MODE_LINEAR = 0, PVD_MODE_CIRCULAR = 1 };
 
+/* pvd_conv_desc flags */
+enum {
+  PVD_PLAN_NO_TMA = 1 /* column passes without TMA staging (register loads only) */
+};
+
 /* pvd_plan_set_kernel flags */
 enum {
   PVD_KERNEL_NORMALIZE = 1 /* divide the kernel by its FP64 sum (on the GPU) */
@@ -84,7 +89,7 @@ typedef struct {
   int mode;           /* PVD_MODE_* */
   int n_kernels;      /* number of kernel slots (nuclides) sharing one forward transform */
   int pad[3];         /* explicit FFT lengths; 0 = choose automatically */
-  int flags;          /* reserved, must be 0 */
+  int flags;          /* PVD_PLAN_* */
 } pvd_conv_desc;
 
 typedef struct {
@@ -141,6 +146,11 @@ pvd_status pvd_conv_execute_weighted(pvd_plan* plan, const float* const* activit
                                      float* dose_d, float out_scale, pvd_stream stream);
 
 pvd_status pvd_plan_destroy(pvd_plan* plan);
+
+/* Device-side status of the plan's passes: PVD_ERR_TIMEOUT if a TMA tile load
+ * of a column pass did not complete within its bounded wait (the pass then
+ * left its tiles unwritten); PVD_OK otherwise.  Synchronises with the device. */
+pvd_status pvd_plan_status(const pvd_plan* plan);
 
 /* Allocation-free convolution.  No counterpart in the reference.
  *

@@ -20,13 +20,15 @@ STATUS_NAMES = {
 PVD_MODE_LINEAR = 0
 PVD_MODE_CIRCULAR = 1
 PVD_KERNEL_NORMALIZE = 1
+PVD_PLAN_NO_TMA = 1
 PVD_MAX_KERNELS = 8
 PVD_MAX_TIMEPOINTS = 16
 
 # Every symbol include/pvd.h declares, in declaration order.
 EXPORTED_SYMBOLS = [
     "pvd_plan_create", "pvd_plan_get_info", "pvd_plan_set_kernel", "pvd_conv_execute",
-    "pvd_conv_execute_host", "pvd_conv_execute_weighted", "pvd_plan_destroy", "pvd_conv_execute_static",
+    "pvd_conv_execute_host", "pvd_conv_execute_weighted", "pvd_plan_destroy", "pvd_plan_status",
+    "pvd_conv_execute_static",
     "pvd_fast_lengths", "pvd_plan_profile", "pvd_plan_pass_times",
     "pvd_weighted_sum", "pvd_tac_fit",
     "pvd_mc_plan_create", "pvd_mc_run", "pvd_mc_plan_destroy",
@@ -102,6 +104,7 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_conv_execute_weighted": (st, [vp, vp, vp, i, vp, vp, f, vp]),
         "pvd_plan_destroy": (st, [vp]),
         "pvd_plan_profile": (st, [vp, i]),
+        "pvd_plan_status": (st, [vp]),
         "pvd_conv_execute_static": (st, [vp, vp, vp, i, i, i, vp, i, i, i, d, i, f, vp]),
         "pvd_fast_lengths": (i, [C.POINTER(C.c_int), i]),
         "pvd_plan_pass_times": (st, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),

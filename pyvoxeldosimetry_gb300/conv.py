@@ -42,10 +42,12 @@ class ConvPlan:
         "reference_circular" (exactly the reference's unpadded circular
         operator, kernel_convolution.py:71-74).
     pad : optional explicit FFT lengths.
+    tma : stage the column passes' tiles with TMA bulk tensor loads (persistent,
+        double-buffered); False uses the register-load passes.
     """
 
     def __init__(self, shape: Sequence[int], kmax: Sequence[int] = (1, 1, 1), n_kernels: int = 1,
-                 mode: str = "linear", pad: Sequence[int] | None = None, device=None):
+                 mode: str = "linear", pad: Sequence[int] | None = None, device=None, tma: bool = True):
         self.device = _require_cuda(device)
         self._lib = N.load()
         if mode not in ("linear", "reference_circular"):
@@ -62,7 +64,7 @@ class ConvPlan:
             d.pad[i] = int(pad[i]) if pad is not None else 0
         d.mode = N.PVD_MODE_LINEAR if mode == "linear" else N.PVD_MODE_CIRCULAR
         d.n_kernels = self.n_kernels
-        d.flags = 0
+        d.flags = 0 if tma else N.PVD_PLAN_NO_TMA
         h = C.c_void_p()
         with torch.cuda.device(self.device):
             N.check(self._lib.pvd_plan_create(C.byref(d), C.byref(h)))
@@ -172,6 +174,10 @@ class ConvPlan:
                                                     int(stream.cuda_stream)))
             stream.synchronize()
         return out
+
+    def status(self) -> None:
+        """Raise if a pass reported a device-side error (a TMA load that timed out)."""
+        N.check(self._lib.pvd_plan_status(self._h))
 
     def close(self) -> None:
         h = getattr(self, "_h", None)

@@ -23,6 +23,8 @@
 // and a symmetric kernel has a real spectrum; CIRCULAR mode puts it at m
 // (the reference's corner placement, truncated to P) which reproduces the
 // reference's K//2 output shift exactly.
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -444,6 +446,14 @@ struct pvd_plan {
   std::vector<void*> allocs;
   // per-pass event timing (instrumentation, off by default)
   int prof = 0;
+  // TMA-staged persistent column passes (register four-step lengths only)
+  int tma = 0;
+  int* d_err = nullptr;
+  CUtensorMap m_yf, m_z;
+  CUtensorMap m_yi[PVD_MAX_KERNELS];
+  int yf_chunks = 1, yf_boxr = 1, yi_chunks = 1, yi_boxr = 1, z_chunks = 1, z_boxr = 1;
+  int grid_yf = 0, grid_yi = 0, grid_z = 0;
+  size_t smem_tyf = 0, smem_tyi = 0, smem_tz = 0;
   // host-buffer execution (pvd_conv_execute_host): device staging and copy streams
   float* io_act = nullptr;
   float* io_rho = nullptr;
@@ -519,10 +529,86 @@ size_t smem_bytes(int L, int nbuf) { return (size_t)(L + nbuf * L * TXP) * sizeo
 
 }  // namespace
 
+namespace {
+
+// rows of one TMA box (<= 256) and the number of boxes covering n rows
+void box_rows(int n, int* chunks, int* boxr) {
+  *chunks = (n + 255) / 256;
+  *boxr = (n + *chunks - 1) / *chunks;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return (PFN_cuTensorMapEncodeTiled_v12000)f;
+  }();
+  return fn;
+}
+
+// [dim2][dim1][HS] complex buffer as 8-byte elements; box {16, b1, b2}
+bool encode_cols(CUtensorMap* m, void* base, int HS, int dim1, int dim2, int b1, int b2) {
+  auto enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)HS, (cuuint64_t)dim1, (cuuint64_t)dim2};
+  const cuuint64_t strides[2] = {(cuuint64_t)HS * 8, (cuuint64_t)HS * 8 * dim1};
+  const cuuint32_t box[3] = {(cuuint32_t)FTX, (cuuint32_t)b1, (cuuint32_t)b2};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+         CUDA_SUCCESS;
+}
+
+int persistent_grid(const void* fn, int threads, size_t smem, int dev) {
+  int nb = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return nb * sms;
+}
+
+// Enables the TMA-staged y and z passes when both axes have register kernels;
+// leaves p->tma = 0 (plain register passes) if anything does not fit.
+pvd_status setup_tma(pvd_plan* p, int smem_max) {
+  const FastLen* fy = p->fl[1];
+  const FastLen* fz = p->fl[0];
+  if (!fy || !fz) return PVD_OK;
+  box_rows(p->N[1], &p->yf_chunks, &p->yf_boxr);
+  box_rows(p->P[1], &p->yi_chunks, &p->yi_boxr);
+  box_rows(p->N[0], &p->z_chunks, &p->z_boxr);
+  p->smem_tyf = tma_y_smem(fy->L, p->yf_chunks, p->yf_boxr);
+  p->smem_tyi = tma_y_smem(fy->L, p->yi_chunks, p->yi_boxr);
+  p->smem_tz = tma_z_smem(fz->L, p->z_chunks, p->z_boxr);
+  if ((int)std::max({p->smem_tyf, p->smem_tyi, p->smem_tz}) > smem_max) return PVD_OK;
+  bool ok = encode_cols(&p->m_yf, p->buf1, p->HS, p->N[1], p->N[0], p->yf_boxr, 1) &&
+            encode_cols(&p->m_z, p->buf2, p->HS, p->P[1], p->N[0], 1, p->z_boxr);
+  for (int s = 0; s < p->nk && ok; ++s) ok = encode_cols(&p->m_yi[s], p->buf3[s], p->HS, p->P[1], p->N[0], p->yi_boxr, 1);
+  if (!ok) return PVD_OK;
+  cudaFuncSetAttribute((const void*)fy->ty_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute((const void*)fy->ty_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  cudaFuncSetAttribute((const void*)fz->tz, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
+  p->grid_yf = persistent_grid((const void*)fy->ty_fwd, fy->threads, p->smem_tyf, p->dev);
+  p->grid_yi = persistent_grid((const void*)fy->ty_inv, fy->threads, p->smem_tyi, p->dev);
+  p->grid_z = persistent_grid((const void*)fz->tz, fz->threads, p->smem_tz, p->dev);
+  if (p->grid_yf <= 0 || p->grid_yi <= 0 || p->grid_z <= 0) return PVD_OK;
+  void* ptr = nullptr;
+  pvd_status st = plan_alloc(p, sizeof(int), &ptr);
+  if (st != PVD_OK) return st;
+  p->d_err = (int*)ptr;
+  cudaError_t e = cudaMemset(p->d_err, 0, sizeof(int));
+  if (e != cudaSuccess) return cuda_error(e, "cudaMemset(status word)");
+  p->tma = 1;
+  return PVD_OK;
+}
+
+}  // namespace
+
 extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
   if (!d || !out) return set_error(PVD_ERR_ARG, "pvd_plan_create: null argument");
   *out = nullptr;
-  if (d->flags != 0) return set_error(PVD_ERR_ARG, "pvd_plan_create: flags must be 0");
+  if (d->flags & ~PVD_PLAN_NO_TMA) return set_error(PVD_ERR_ARG, "pvd_plan_create: unknown flags");
   if (d->mode != PVD_MODE_LINEAR && d->mode != PVD_MODE_CIRCULAR)
     return set_error(PVD_ERR_ARG, "pvd_plan_create: unknown mode");
   if (d->n_kernels < 1 || d->n_kernels > PVD_MAX_KERNELS)
@@ -621,6 +707,7 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
     for (int s = 1; s < p->nk && e == cudaSuccess; ++s) e = cudaMemset(p->buf3[s], 0, b2);
     if (e != cudaSuccess) st = cuda_error(e, "cudaMemset(workspace)");
   }
+  if (st == PVD_OK && !(d->flags & PVD_PLAN_NO_TMA)) st = setup_tma(p, smem_max);
   if (st != PVD_OK) {
     plan_free(p);
     delete p;
@@ -811,7 +898,10 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
     }
     {
       PassTimer t(p, 1, st);
-      if (fy)
+      if (p->tma)
+        fy->ty_fwd<<<std::min(p->grid_yf, ctiles * (z1 - z0)), fy->threads, p->smem_tyf, st>>>(
+            p->m_yf, p->buf2, N1, p->P[1], z0, z1 - z0, ctiles, p->HS, p->yf_chunks, p->yf_boxr, p->tw[1], p->d_err);
+      else if (fy)
         fy->y_fwd<<<dim3(ctiles, z1 - z0), fy->threads, fy->smem_col, st>>>(b1, b2, N1, p->P[1], p->HS, p->tw[1]);
       else
         k_y<false><<<dim3(ctiles, z1 - z0), NT, p->smem_y, st>>>(b1, b2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
@@ -838,7 +928,10 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
       os.mode[i] = p->spec_mode[s];
     }
     PassTimer t(p, 2, st);
-    if (fz)
+    if (p->tma)
+      fz->tz<<<std::min(p->grid_z, ctiles * p->P[1]), fz->threads, p->smem_tz, st>>>(
+          p->m_z, os, N0, p->P[1], p->HS, ctiles, p->z_chunks, p->z_boxr, p->tw[0], p->d_err);
+    else if (fz)
       fz->z<<<dim3(ctiles, p->P[1]), fz->threads, fz->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->tw[0]);
     else
       k_z<<<dim3(ctiles, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
@@ -849,7 +942,10 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
     if (hio && s == 0 && hio->rho) PVD_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_rho, 0));
     {
       PassTimer t(p, 3, st);
-      if (fy)
+      if (p->tma)
+        fy->ty_inv<<<std::min(p->grid_yi, ctiles * N0), fy->threads, p->smem_tyi, st>>>(
+            p->m_yi[s], p->buf1, p->P[1], N1, 0, N0, ctiles, p->HS, p->yi_chunks, p->yi_boxr, p->tw[1], p->d_err);
+      else if (fy)
         fy->y_inv<<<dim3(ctiles, N0), fy->threads, fy->smem_col, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS,
                                                                        p->tw[1]);
       else
@@ -988,6 +1084,15 @@ extern "C" pvd_status pvd_plan_pass_times(pvd_plan* p, double* ms, int* launches
     ms[r.kind] += t;
     launches[r.kind] += 1;
   }
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_plan_status(const pvd_plan* p) {
+  if (!p) return set_error(PVD_ERR_ARG, "pvd_plan_status: null plan");
+  if (!p->d_err) return PVD_OK;
+  int v = 0;
+  PVD_CUDA_TRY(cudaMemcpy(&v, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (v) return set_error((pvd_status)v, "pvd_plan_status: a TMA tile load did not complete in time");
   return PVD_OK;
 }
 

@@ -12,6 +12,7 @@
 
 #include "conv_types.cuh"
 #include "fft_reg.cuh"
+#include "tma.cuh"
 
 namespace pvd {
 
@@ -25,6 +26,12 @@ typedef void (*KxFwdFn)(ActIn, float2*, int, int, int, const float2*);
 typedef void (*KxInvFn)(const float2*, float*, const float*, int, int, int, float, const float2*);
 typedef void (*KyFn)(const float2*, float2*, int, int, int, const float2*);
 typedef void (*KzFn)(const float2*, OutSet, int, int, int, const float2*);
+// TMA-staged persistent column passes
+typedef void (*KtyFn)(const __grid_constant__ CUtensorMap, float2*, int, int, int, int, int, int, int, int,
+                      const float2*, int*);
+typedef void (*KtzFn)(const __grid_constant__ CUtensorMap, OutSet, int, int, int, int, int, int, const float2*, int*);
+
+constexpr unsigned long long TMA_WAIT_NS = 2000000000ull;  // a tile that has not landed after 2 s is an error
 
 struct FastLen {
   int L, A, B, threads;
@@ -33,6 +40,8 @@ struct FastLen {
   KxInvFn x_inv;
   KyFn y_fwd, y_inv;
   KzFn z;
+  KtyFn ty_fwd, ty_inv;
+  KtzFn tz;
 };
 
 // shared-memory layout helpers: twiddle table first (rounded to 2 float2 = 16 B)
@@ -161,6 +170,196 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), z_min_blocks(A, B)) kf_z(cons
       }
     }
   });
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged persistent column passes.  Each CTA walks tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ...; while it transforms tile t from one shared
+// stage, one elected thread has already issued the bulk tensor load of the
+// next tile into the other stage (mbarrier-completed), so HBM latency overlaps
+// the FFT arithmetic.  A stage is (chunks * boxr) rows of FTX complex (128 B
+// per row), at least L rows so it can double as the exchange tile.  Waits are
+// bounded: a load that has not landed after TMA_WAIT_NS sets *err and the CTA
+// leaves.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tma_issue_rows(float2* dst, const CUtensorMap* map, int c0, int c2_or_row,
+                                               bool rows_on_dim1, int chunks, int boxr, uint64_t* bar) {
+  fence_proxy_async_shared();
+  mbar_arrive_expect_tx(bar, (uint32_t)(chunks * boxr * FTX * sizeof(float2)));
+  for (int k = 0; k < chunks; ++k) {
+    if (rows_on_dim1)
+      tma_load_3d(dst + k * boxr * FTX, map, c0, k * boxr, c2_or_row, bar);
+    else
+      tma_load_3d(dst + k * boxr * FTX, map, c0, c2_or_row, k * boxr, bar);
+  }
+}
+
+// y pass: tiles (column tile, z slab) of a [nslab][nin][HS] tensor -> [nslab][nout][HS]
+template <int A, int B, bool INV>
+__global__ void __launch_bounds__(FTX* cmax(A, B)) kt_y(const __grid_constant__ CUtensorMap tin,
+                                                         float2* __restrict__ out, int nin, int nout, int slab0,
+                                                         int nslab, int ctiles, int HS, int chunks, int boxr,
+                                                         const float2* __restrict__ twg, int* __restrict__ err) {
+  constexpr int L = A * B, NTH = FTX * cmax(A, B);
+  extern __shared__ __align__(128) float2 sm[];
+  const int SR = max(chunks * boxr, L);
+  float2* tw = sm + 2 * SR * FTX;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + tw_slots(L));
+  const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
+  const int total = ctiles * nslab;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  load_tw<L>(tw, twg, NTH);
+  __syncthreads();
+  int t = blockIdx.x;
+  if (threadIdx.x == 0 && t < total)
+    tma_issue_rows(sm, &tin, (t % ctiles) * FTX, slab0 + t / ctiles, true, chunks, boxr, &bar[0]);
+  for (int i = 0; t < total; ++i, t += gridDim.x) {
+    const int s = i & 1;
+    const int tn = t + gridDim.x;
+    if (threadIdx.x == 0 && tn < total)
+      tma_issue_rows(sm + (s ^ 1) * SR * FTX, &tin, (tn % ctiles) * FTX, slab0 + tn / ctiles, true, chunks, boxr,
+                     &bar[s ^ 1]);
+    const bool ok = mbar_wait_bounded(&bar[s], (i >> 1) & 1, TMA_WAIT_NS);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(err, (int)PVD_ERR_TIMEOUT);
+      return;
+    }
+    float2* stage = sm + s * SR * FTX;
+    float2 v[B];
+    if (j < A) {
+      static_for<B>([&](auto ib) {
+        constexpr int b = decltype(ib)::value;
+        const int n = j + A * b;
+        v[b] = (n < nin) ? stage[n * FTX + c] : make_float2(0.f, 0.f);
+      });
+    }
+    float2 w[A];
+    four_step<A, B, INV, FTX, true>(v, w, stage, tw, c, j);
+    float2* dst = out + (long long)(slab0 + t / ctiles) * nout * HS + (t % ctiles) * FTX + c;
+    if (j < B) {
+      static_for<A>([&](auto iq) {
+        constexpr int q = decltype(iq)::value;
+        const int k = j + B * q;
+        if (k < nout) dst[(long long)k * HS] = w[q];
+      });
+    }
+    __syncthreads();  // the stage (also the exchange tile) is free for the load after next
+  }
+}
+
+// z pass: tiles (column tile, ky) of a [N0][P1][HS] tensor, rows along z
+template <int A, int B>
+__global__ void __launch_bounds__(FTX* cmax(A, B), z_min_blocks(A, B)) kt_z(const __grid_constant__ CUtensorMap tin,
+                                                                            OutSet os, int N0, int P1, int HS,
+                                                                            int ctiles, int chunks, int boxr,
+                                                                            const float2* __restrict__ twg,
+                                                                            int* __restrict__ err) {
+  constexpr int L = A * B, NTH = FTX * cmax(A, B);
+  extern __shared__ __align__(128) float2 sm[];
+  const int SR = max(chunks * boxr, L);
+  float2* ex = sm + 2 * SR * FTX;
+  float2* tw = ex + L * FTX;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tw + tw_slots(L));
+  const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
+  const int total = ctiles * P1;
+  const long long zstride = (long long)P1 * HS;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  load_tw<L>(tw, twg, NTH);
+  __syncthreads();
+  int t = blockIdx.x;
+  if (threadIdx.x == 0 && t < total) tma_issue_rows(sm, &tin, (t % ctiles) * FTX, t / ctiles, false, chunks, boxr, &bar[0]);
+  for (int i = 0; t < total; ++i, t += gridDim.x) {
+    const int s = i & 1;
+    const int tn = t + gridDim.x;
+    if (threadIdx.x == 0 && tn < total)
+      tma_issue_rows(sm + (s ^ 1) * SR * FTX, &tin, (tn % ctiles) * FTX, tn / ctiles, false, chunks, boxr,
+                     &bar[s ^ 1]);
+    const bool ok = mbar_wait_bounded(&bar[s], (i >> 1) & 1, TMA_WAIT_NS);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(err, (int)PVD_ERR_TIMEOUT);
+      return;
+    }
+    float2* stage = sm + s * SR * FTX;
+    const int kx0 = (t % ctiles) * FTX, ky = t / ctiles;
+    const long long base = (long long)ky * HS + kx0 + c;
+    float2 v[B];
+    if (j < A) {
+      static_for<B>([&](auto ib) {
+        constexpr int b = decltype(ib)::value;
+        const int n = j + A * b;
+        v[b] = (n < N0) ? stage[n * FTX + c] : make_float2(0.f, 0.f);
+      });
+    }
+    {
+      float2 X[A];
+      four_step<A, B, false, FTX, false>(v, X, ex, tw, c, j);
+      // every stage read happened before four_step's barrier: the stage now keeps the spectrum
+      if (j < B) {
+        static_for<A>([&](auto iq) {
+          constexpr int q = decltype(iq)::value;
+          stage[(j + B * q) * FTX + c] = X[q];
+        });
+      }
+    }
+    static_for<FZ_SLOTS>([&](auto is) {
+      constexpr int sl = decltype(is)::value;
+      if (sl < os.n) {
+        float2 X[A], Y[A];
+        if (j < B) {
+          static_for<A>([&](auto iq) {
+            constexpr int q = decltype(iq)::value;
+            X[q] = stage[(j + B * q) * FTX + c];
+          });
+          if (os.mode[sl] == SPEC_REAL_EVEN) {
+            const float* S = (const float*)os.s[sl];
+            static_for<A>([&](auto iq) {
+              constexpr int q = decltype(iq)::value;
+              const int kz = j + B * q;
+              const int kzq = min(kz, os.P0 - kz), kyq = min(ky, P1 - ky);
+              Y[q] = cscale(X[q], __ldg(S + ((long long)kzq * os.P1h + kyq) * HS + kx0 + c));
+            });
+          } else {
+            const float2* S = (const float2*)os.s[sl];
+            static_for<A>([&](auto iq) {
+              constexpr int q = decltype(iq)::value;
+              const int kz = j + B * q;
+              Y[q] = cmul(X[q], __ldg(S + ((long long)kz * P1 + ky) * HS + kx0 + c));
+            });
+          }
+        }
+        __syncthreads();  // previous exchange reads are done
+        float2 Z[B];
+        four_step<B, A, true, FTX, false>(Y, Z, ex, tw, c, j);
+        if (j < A) {
+          float2* dst = os.p[sl] + base;
+          static_for<B>([&](auto ir) {
+            constexpr int r = decltype(ir)::value;
+            const int z = j + A * r;
+            if (z < N0) dst[z * zstride] = Z[r];
+          });
+        }
+      }
+    });
+    __syncthreads();  // stage and exchange free
+  }
+}
+
+// shared bytes of the TMA passes (stages of SR rows, twiddles, two barriers)
+inline size_t tma_y_smem(int L, int chunks, int boxr) {
+  const int SR = chunks * boxr > L ? chunks * boxr : L;
+  return sizeof(float2) * ((size_t)2 * SR * FTX + tw_slots(L)) + 2 * sizeof(uint64_t);
+}
+inline size_t tma_z_smem(int L, int chunks, int boxr) {
+  const int SR = chunks * boxr > L ? chunks * boxr : L;
+  return sizeof(float2) * ((size_t)2 * SR * FTX + (size_t)L * FTX + tw_slots(L)) + 2 * sizeof(uint64_t);
 }
 
 // ---------------------------------------------------------------------------
@@ -369,6 +568,9 @@ FastLen make_fast_len() {
   f.y_fwd = kf_y<A, B, false>;
   f.y_inv = kf_y<A, B, true>;
   f.z = kf_z<A, B>;
+  f.ty_fwd = kt_y<A, B, false>;
+  f.ty_inv = kt_y<A, B, true>;
+  f.tz = kt_z<A, B>;
   return f;
 }
 

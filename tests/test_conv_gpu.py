@@ -22,16 +22,18 @@ def rel_err(d, ref):
     return float(np.abs(d - ref).max() / scale) if scale > 0 else float(np.abs(d).max())
 
 
-def run_plan(a, kernels, mode="linear", density=None, out_scale=1.0, normalize=False, scales=None, pad=None):
+def run_plan(a, kernels, mode="linear", density=None, out_scale=1.0, normalize=False, scales=None, pad=None,
+             tma=True):
     from pyvoxeldosimetry_gb300.conv import ConvPlan
     kmax = tuple(max(k.shape[i] for k in kernels) for i in range(3))
-    with ConvPlan(a.shape, kmax=kmax, n_kernels=len(kernels), mode=mode, pad=pad) as p:
+    with ConvPlan(a.shape, kmax=kmax, n_kernels=len(kernels), mode=mode, pad=pad, tma=tma) as p:
         for s, k in enumerate(kernels):
             p.set_kernel(s, k, scale=1.0 if scales is None else scales[s], normalize=normalize)
         at = torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
         rt = None if density is None else torch.from_numpy(np.ascontiguousarray(density, np.float32)).cuda()
         out = p.execute(at, density=rt, out_scale=out_scale)
         torch.cuda.synchronize()
+        p.status()
         return out.cpu().numpy().astype(np.float64)
 
 
@@ -145,8 +147,9 @@ FAST_LENGTHS = [64, 72, 80, 96, 112, 128, 144, 160, 192, 224, 240, 252, 256, 270
                 360, 384, 400, 448, 480, 512, 560, 576, 640]
 
 
+@pytest.mark.parametrize("tma", [True, False])
 @pytest.mark.parametrize("L", FAST_LENGTHS)
-def test_every_fast_length_on_every_axis(L):
+def test_every_fast_length_on_every_axis(L, tma):
     """Force FFT length L on all three axes (small volume): exercises the register
     four-step x/y/z pass kernels of that length with a real-even (radial) kernel
     and a complex-spectrum (asymmetric) kernel in one plan."""
@@ -155,18 +158,32 @@ def test_every_fast_length_on_every_axis(L):
     shape = (min(L - 8, 37), min(L - 8, 20), min(L - 8, 45))
     a = rng.random(shape)
     ks = [radial_kernel(9, 1.8, 1.5), rng.random((5, 7, 3))]
-    d = run_plan(a, ks, pad=(L, L, L))
+    d = run_plan(a, ks, pad=(L, L, L), tma=tma)
     for s, k in enumerate(ks):
         assert rel_err(d[s], oc.linear_conv_same(a, k)) <= TOL
 
 
-def test_fast_full_extent_and_many_slots():
+@pytest.mark.parametrize("tma", [True, False])
+def test_fast_full_extent_and_many_slots(tma):
     """N = P - K + 1 on the 280 axis (no slack in the padding) and more kernel slots
     than one fast z launch takes (slot 0 transforms in place and must run last)."""
     rng = np.random.default_rng(21)
     shape = (260, 12, 24)
     a = rng.random(shape)
     ks = [radial_kernel(21, 1.8, 1.5)] + [rng.random((3, 3, 3)) for _ in range(5)] + [radial_kernel(11, 0.5, 1.5)]
-    d = run_plan(a, ks, pad=(280, 64, 64))
+    d = run_plan(a, ks, pad=(280, 64, 64), tma=tma)
+    for s, k in enumerate(ks):
+        assert rel_err(d[s], oc.linear_conv_same(a, k)) <= TOL
+
+
+@pytest.mark.parametrize("tma", [True, False])
+def test_tma_boxes_split_long_columns(tma):
+    """Columns longer than one 256-row TMA box (N1 = 300, P1 = 320, N0 = 270) take
+    several boxes per tile; both column-pass variants agree with the oracle."""
+    rng = np.random.default_rng(31)
+    shape = (270, 300, 20)
+    a = rng.random(shape)
+    ks = [radial_kernel(9, 1.0, 1.5), rng.random((3, 5, 3))]
+    d = run_plan(a, ks, pad=(280, 320, 64), tma=tma)
     for s, k in enumerate(ks):
         assert rel_err(d[s], oc.linear_conv_same(a, k)) <= TOL
