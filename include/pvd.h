@@ -72,7 +72,8 @@ enum { PVD_MODE_LINEAR = 0, PVD_MODE_CIRCULAR = 1 };
 
 /* pvd_conv_desc flags */
 enum {
-  PVD_PLAN_NO_TMA = 1 /* column passes without TMA staging (register loads only) */
+  PVD_PLAN_TMA = 1 /* stage the column passes' tiles with TMA bulk tensor loads (persistent,
+                      double-buffered); default: tiles loaded straight into registers */
 };
 
 /* pvd_plan_set_kernel flags */

@@ -20,7 +20,7 @@ STATUS_NAMES = {
 PVD_MODE_LINEAR = 0
 PVD_MODE_CIRCULAR = 1
 PVD_KERNEL_NORMALIZE = 1
-PVD_PLAN_NO_TMA = 1
+PVD_PLAN_TMA = 1
 PVD_MAX_KERNELS = 8
 PVD_MAX_TIMEPOINTS = 16
 

@@ -578,6 +578,9 @@ pvd_status setup_tma(pvd_plan* p, int smem_max) {
   box_rows(p->N[1], &p->yf_chunks, &p->yf_boxr);
   box_rows(p->P[1], &p->yi_chunks, &p->yi_boxr);
   box_rows(p->N[0], &p->z_chunks, &p->z_boxr);
+  // each box lands at stage + k * boxr rows: 128-byte aligned only if a box of rows is
+  for (int br : {p->yf_boxr, p->yi_boxr, p->z_boxr})
+    if (((size_t)br * FTX * sizeof(float2)) % 128 != 0) return PVD_OK;
   p->smem_tyf = tma_y_smem(fy->L, p->yf_chunks, p->yf_boxr);
   p->smem_tyi = tma_y_smem(fy->L, p->yi_chunks, p->yi_boxr);
   p->smem_tz = tma_z_smem(fz->L, p->z_chunks, p->z_boxr);
@@ -608,7 +611,7 @@ pvd_status setup_tma(pvd_plan* p, int smem_max) {
 extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
   if (!d || !out) return set_error(PVD_ERR_ARG, "pvd_plan_create: null argument");
   *out = nullptr;
-  if (d->flags & ~PVD_PLAN_NO_TMA) return set_error(PVD_ERR_ARG, "pvd_plan_create: unknown flags");
+  if (d->flags & ~PVD_PLAN_TMA) return set_error(PVD_ERR_ARG, "pvd_plan_create: unknown flags");
   if (d->mode != PVD_MODE_LINEAR && d->mode != PVD_MODE_CIRCULAR)
     return set_error(PVD_ERR_ARG, "pvd_plan_create: unknown mode");
   if (d->n_kernels < 1 || d->n_kernels > PVD_MAX_KERNELS)
@@ -707,7 +710,7 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
     for (int s = 1; s < p->nk && e == cudaSuccess; ++s) e = cudaMemset(p->buf3[s], 0, b2);
     if (e != cudaSuccess) st = cuda_error(e, "cudaMemset(workspace)");
   }
-  if (st == PVD_OK && !(d->flags & PVD_PLAN_NO_TMA)) st = setup_tma(p, smem_max);
+  if (st == PVD_OK && (d->flags & PVD_PLAN_TMA)) st = setup_tma(p, smem_max);
   if (st != PVD_OK) {
     plan_free(p);
     delete p;
@@ -870,11 +873,13 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
   const int N0 = p->N[0], N1 = p->N[1], N2 = p->N[2];
   const int nrows = N0 * N1;
   const long long vox = (long long)nrows * N2;
-  const int ctiles = p->HS / TX;
-
   const FastLen* fx = p->fl[2];
   const FastLen* fy = p->fl[1];
   const FastLen* fz = p->fl[0];
+  // column tiles and row blocks differ between the register (FTX) and generic (TX) kernels
+  const int ctiles_y = p->HS / (fy ? FTX : TX);
+  const int ctiles_z = p->HS / (fz ? FTX : TX);
+  const int rows_x = 2 * (fx ? FTX : TX);
   // forward x and y passes, in z chunks when the activity arrives from the host
   // in pieces (each chunk waits for its own upload)
   const int nchunks = hio ? std::min(PVD_HOST_CHUNKS, N0) : 1;
@@ -885,7 +890,7 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
     ActIn ic = in;
     for (int t = 0; t < ic.n; ++t) ic.p[t] = in.p[t] + (long long)z0 * N1 * N2;
     const int rows = (z1 - z0) * N1;
-    const int xb = (rows + 2 * TX - 1) / (2 * TX);
+    const int xb = (rows + rows_x - 1) / rows_x;
     float2* b1 = p->buf1 + (long long)z0 * N1 * p->HS;
     float2* b2 = p->buf2 + (long long)z0 * p->P[1] * p->HS;
     {
@@ -899,12 +904,12 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
     {
       PassTimer t(p, 1, st);
       if (p->tma)
-        fy->ty_fwd<<<std::min(p->grid_yf, ctiles * (z1 - z0)), fy->threads, p->smem_tyf, st>>>(
-            p->m_yf, p->buf2, N1, p->P[1], z0, z1 - z0, ctiles, p->HS, p->yf_chunks, p->yf_boxr, p->tw[1], p->d_err);
+        fy->ty_fwd<<<std::min(p->grid_yf, ctiles_y * (z1 - z0)), fy->threads, p->smem_tyf, st>>>(
+            p->m_yf, p->buf2, N1, p->P[1], z0, z1 - z0, ctiles_y, p->HS, p->yf_chunks, p->yf_boxr, p->tw[1], p->d_err);
       else if (fy)
-        fy->y_fwd<<<dim3(ctiles, z1 - z0), fy->threads, fy->smem_col, st>>>(b1, b2, N1, p->P[1], p->HS, p->tw[1]);
+        fy->y_fwd<<<dim3(ctiles_y, z1 - z0), fy->threads, fy->smem_col, st>>>(b1, b2, N1, p->P[1], p->HS, p->tw[1]);
       else
-        k_y<false><<<dim3(ctiles, z1 - z0), NT, p->smem_y, st>>>(b1, b2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
+        k_y<false><<<dim3(ctiles_y, z1 - z0), NT, p->smem_y, st>>>(b1, b2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
       PVD_LAUNCH_CHECK("y_fwd");
     }
   }
@@ -929,27 +934,27 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
     }
     PassTimer t(p, 2, st);
     if (p->tma)
-      fz->tz<<<std::min(p->grid_z, ctiles * p->P[1]), fz->threads, p->smem_tz, st>>>(
-          p->m_z, os, N0, p->P[1], p->HS, ctiles, p->z_chunks, p->z_boxr, p->tw[0], p->d_err);
+      fz->tz<<<std::min(p->grid_z, ctiles_z * p->P[1]), fz->threads, p->smem_tz, st>>>(
+          p->m_z, os, N0, p->P[1], p->HS, ctiles_z, p->z_chunks, p->z_boxr, p->tw[0], p->d_err);
     else if (fz)
-      fz->z<<<dim3(ctiles, p->P[1]), fz->threads, fz->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->tw[0]);
+      fz->z<<<dim3(ctiles_z, p->P[1]), fz->threads, fz->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->tw[0]);
     else
-      k_z<<<dim3(ctiles, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
+      k_z<<<dim3(ctiles_z, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
     PVD_LAUNCH_CHECK("z");
   }
-  const int xblocks = (nrows + 2 * TX - 1) / (2 * TX);
+  const int xblocks = (nrows + rows_x - 1) / rows_x;
   for (int s = 0; s < p->nk; ++s) {
     if (hio && s == 0 && hio->rho) PVD_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_rho, 0));
     {
       PassTimer t(p, 3, st);
       if (p->tma)
-        fy->ty_inv<<<std::min(p->grid_yi, ctiles * N0), fy->threads, p->smem_tyi, st>>>(
-            p->m_yi[s], p->buf1, p->P[1], N1, 0, N0, ctiles, p->HS, p->yi_chunks, p->yi_boxr, p->tw[1], p->d_err);
+        fy->ty_inv<<<std::min(p->grid_yi, ctiles_y * N0), fy->threads, p->smem_tyi, st>>>(
+            p->m_yi[s], p->buf1, p->P[1], N1, 0, N0, ctiles_y, p->HS, p->yi_chunks, p->yi_boxr, p->tw[1], p->d_err);
       else if (fy)
-        fy->y_inv<<<dim3(ctiles, N0), fy->threads, fy->smem_col, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS,
+        fy->y_inv<<<dim3(ctiles_y, N0), fy->threads, fy->smem_col, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS,
                                                                        p->tw[1]);
       else
-        k_y<true><<<dim3(ctiles, N0), NT, p->smem_y, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS, p->f[1],
+        k_y<true><<<dim3(ctiles_y, N0), NT, p->smem_y, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS, p->f[1],
                                                            p->tw[1]);
       PVD_LAUNCH_CHECK("y_inv");
     }

@@ -16,7 +16,7 @@
 
 namespace pvd {
 
-constexpr int FTX = 16;        // transforms per CTA
+constexpr int FTX = 16;        // transforms (columns / row pairs) per CTA
 constexpr int FTXP = FTX + 1;  // padded stride of row-pass staging tiles
 constexpr int FZ_SLOTS = 4;    // kernel slots per z-pass launch
 
@@ -91,9 +91,11 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_y(const float2* __restrict
 // z pass: forward, spectrum multiply, inverse, crop — every kernel slot.
 // blockIdx.x = column tile, blockIdx.y = ky.
 // ---------------------------------------------------------------------------
-// 3 resident CTAs per SM where the register arrays allow it without spilling
-// (A + B <= 36: at most 64 registers at 320 threads); the compiler's choice otherwise
-__host__ __device__ constexpr int z_min_blocks(int a, int b) { return (a + b <= 36 && cmax(a, b) <= 20) ? 3 : 1; }
+// enough resident CTAs for ~960 threads per SM where the register arrays allow it
+// without spilling (A + B <= 36 fits in 64 registers); the compiler's choice otherwise
+__host__ __device__ constexpr int z_min_blocks(int a, int b) {
+  return (a + b <= 36 && cmax(a, b) <= 20) ? 960 / (FTX * cmax(a, b)) : 1;
+}
 
 template <int A, int B>
 __global__ void __launch_bounds__(FTX* cmax(A, B), z_min_blocks(A, B)) kf_z(const float2* __restrict__ in, OutSet os, int N0, int P1,
@@ -182,6 +184,10 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), z_min_blocks(A, B)) kf_z(cons
 // bounded: a load that has not landed after TMA_WAIT_NS sets *err and the CTA
 // leaves.
 // ---------------------------------------------------------------------------
+// Every chunk of a stage starts at a multiple of one 128-byte row, the alignment
+// bulk tensor copies need for their shared-memory destination.
+static_assert(FTX * sizeof(float2) % 128 == 0, "TMA stage rows must be multiples of 128 bytes");
+
 __device__ __forceinline__ void tma_issue_rows(float2* dst, const CUtensorMap* map, int c0, int c2_or_row,
                                                bool rows_on_dim1, int chunks, int boxr, uint64_t* bar) {
   fence_proxy_async_shared();
@@ -365,11 +371,11 @@ inline size_t tma_z_smem(int L, int chunks, int boxr) {
 // ---------------------------------------------------------------------------
 // Row passes (x axis, contiguous).  A CTA owns ROWS = 2*FTX consecutive rows:
 // a contiguous block of global memory, moved with fully coalesced loads that
-// keep XU loads per thread in flight.  Shared tiles use odd row strides so the
+// keep all of a row's loads per lane in flight (trip counts are compile-time,
+// from L).  Shared tiles use odd row strides so the
 // transposed per-transform reads of the four-step FFT are bank-conflict free.
 // Real rows 2m and 2m+1 form the real and imaginary part of transform m.
 // ---------------------------------------------------------------------------
-constexpr int XU = 8;
 
 // x forward: weighted timepoint sum, zero pad, R2C, half spectra [row][HS].
 template <int A, int B>
@@ -386,28 +392,36 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_fwd(ActIn in, float2* __
   const long long row0 = (long long)blockIdx.x * ROWS;
   const int nr = (int)min((long long)ROWS, (long long)nrows - row0);
   load_tw<L>(tw, twg, NTH);
-  // whole warps take whole rows: lane-contiguous loads, XU per lane in flight
+  // whole warps take whole rows: lane-contiguous loads, the row's loads all in flight
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int NU = (L + 31) / 32;  // N2 <= L: row slots per lane
   if (warp < NWF) {
     for (int rr = warp; rr < nr; rr += NWF) {
-      for (int n0 = 0; n0 < N2; n0 += 32 * XU) {
-        float r[XU];
+      float r[NU];
+      if (in.n == 1) {  // one activity map (the common case): plain loads
+        const float* src = in.p[0] + (row0 + rr) * N2;
 #pragma unroll
-        for (int u = 0; u < XU; ++u) r[u] = 0.f;
+        for (int u = 0; u < NU; ++u) {
+          const int n = 32 * u + lane;
+          r[u] = (n < N2) ? __ldg(src + n) : 0.f;
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < NU; ++u) r[u] = 0.f;
         for (int t = 0; t < in.n; ++t) {
           const float* src = in.p[t] + (row0 + rr) * N2;
           const float w = in.w[t];
 #pragma unroll
-          for (int u = 0; u < XU; ++u) {
-            const int n = n0 + 32 * u + lane;
+          for (int u = 0; u < NU; ++u) {
+            const int n = 32 * u + lane;
             if (n < N2) r[u] += w * __ldg(src + n);
           }
         }
+      }
 #pragma unroll
-        for (int u = 0; u < XU; ++u) {
-          const int n = n0 + 32 * u + lane;
-          if (n < N2) chunk[rr * S + n] = r[u];
-        }
+      for (int u = 0; u < NU; ++u) {
+        const int n = 32 * u + lane;
+        if (n < N2) chunk[rr * S + n] = r[u];
       }
     }
   }
@@ -442,12 +456,17 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_fwd(ActIn in, float2* __
       const int m = rr >> 1;
       const bool odd = rr & 1;
       float2* dst = out + (row0 + rr) * HS;
-      for (int k = lane; k < H; k += 32) {
-        const float2 z1 = buf[m * S2 + k];
-        const float2 z2 = buf[m * S2 + (k ? L - k : 0)];
-        // Xa = (Z[k] + conj Z[-k]) / 2 ;  Xb = (Z[k] - conj Z[-k]) / (2i)
-        dst[k] = odd ? make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x))
-                     : make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+      constexpr int KU = (H + 31) / 32;
+#pragma unroll
+      for (int u = 0; u < KU; ++u) {
+        const int k = 32 * u + lane;
+        if (k < H) {
+          const float2 z1 = buf[m * S2 + k];
+          const float2 z2 = buf[m * S2 + (k ? L - k : 0)];
+          // Xa = (Z[k] + conj Z[-k]) / 2 ;  Xb = (Z[k] - conj Z[-k]) / (2i)
+          dst[k] = odd ? make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x))
+                       : make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
+        }
       }
     }
   }
@@ -476,18 +495,17 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_inv(const float2* __rest
     for (int rr = warp; rr < nr; rr += NWF) {
       const float2* src = in + (row0 + rr) * HS;
       float2* dsm = ((rr & 1) ? hb : ha) + (rr >> 1) * S2;
-      for (int k0 = 0; k0 < H; k0 += 32 * XU) {
-        float2 r[XU];
+      constexpr int KU = (H + 31) / 32;
+      float2 r[KU];
 #pragma unroll
-        for (int u = 0; u < XU; ++u) {
-          const int k = k0 + 32 * u + lane;
-          if (k < H) r[u] = src[k];
-        }
+      for (int u = 0; u < KU; ++u) {
+        const int k = 32 * u + lane;
+        if (k < H) r[u] = src[k];
+      }
 #pragma unroll
-        for (int u = 0; u < XU; ++u) {
-          const int k = k0 + 32 * u + lane;
-          if (k < H) dsm[k] = r[u];
-        }
+      for (int u = 0; u < KU; ++u) {
+        const int k = 32 * u + lane;
+        if (k < H) dsm[k] = r[u];
       }
     }
   }
@@ -529,23 +547,22 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_inv(const float2* __rest
     for (int rr = warp; rr < nr; rr += NWF) {
       float* dst = out + (row0 + rr) * N2;
       const float* dr = rho ? rho + (row0 + rr) * N2 : nullptr;
-      for (int n0 = 0; n0 < N2; n0 += 32 * XU) {
-        float d[XU];
-        if (dr) {
+      constexpr int NU = (L + 31) / 32;  // N2 <= L
+      float d[NU];
+      if (dr) {
 #pragma unroll
-          for (int u = 0; u < XU; ++u) {
-            const int n = n0 + 32 * u + lane;
-            d[u] = (n < N2) ? __ldg(dr + n) : 1.f;
-          }
+        for (int u = 0; u < NU; ++u) {
+          const int n = 32 * u + lane;
+          d[u] = (n < N2) ? __ldg(dr + n) : 1.f;
         }
+      }
 #pragma unroll
-        for (int u = 0; u < XU; ++u) {
-          const int n = n0 + 32 * u + lane;
-          if (n < N2) {
-            float val = oc[rr * S + n];
-            if (dr) val = (d[u] > 0.f) ? val / d[u] : 0.f;
-            dst[n] = val;
-          }
+      for (int u = 0; u < NU; ++u) {
+        const int n = 32 * u + lane;
+        if (n < N2) {
+          float val = oc[rr * S + n];
+          if (dr) val = (d[u] > 0.f) ? val * __frcp_rn(d[u]) : 0.f;
+          dst[n] = val;
         }
       }
     }
