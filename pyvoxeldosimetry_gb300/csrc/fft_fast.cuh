@@ -378,8 +378,14 @@ inline size_t tma_z_smem(int L, int chunks, int boxr) {
 // ---------------------------------------------------------------------------
 
 // x forward: weighted timepoint sum, zero pad, R2C, half spectra [row][HS].
+// row passes of up to 320 threads keep ~1280 threads resident per SM (4 CTAs of
+// 320: <= 51 registers); larger tiles are left to the compiler
+__host__ __device__ constexpr int x_min_blocks(int a, int b) {
+  return FTX * cmax(a, b) <= 320 ? 1280 / (FTX * cmax(a, b)) : 1;
+}
+
 template <int A, int B>
-__global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_fwd(ActIn in, float2* __restrict__ out, int nrows, int N2,
+__global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_fwd(ActIn in, float2* __restrict__ out, int nrows, int N2,
                                                              int HS, const float2* __restrict__ twg) {
   constexpr int L = A * B, NTH = FTX * cmax(A, B), H = L / 2 + 1, ROWS = 2 * FTX;
   constexpr int NWF = NTH / 32;  // full warps (the last warp is partial when max(A, B) is odd)
@@ -474,7 +480,7 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_fwd(ActIn in, float2* __
 
 // x inverse: C2R of pairs of half-spectrum rows, crop, scale, density.
 template <int A, int B>
-__global__ void __launch_bounds__(FTX* cmax(A, B)) kf_x_inv(const float2* __restrict__ in, float* __restrict__ out,
+__global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_inv(const float2* __restrict__ in, float* __restrict__ out,
                                                              const float* __restrict__ rho, int nrows, int N2, int HS,
                                                              float scale, const float2* __restrict__ twg) {
   constexpr int L = A * B, NTH = FTX * cmax(A, B), H = L / 2 + 1, ROWS = 2 * FTX;
