@@ -227,11 +227,26 @@ enum {
   PVD_FIT_MONO_LAMBDA = 0, PVD_FIT_F2 = 1, PVD_FIT_F3 = 2, PVD_FIT_F3A = 3, PVD_FIT_F4A = 4,
   PVD_FIT_F4B = 5, PVD_FIT_F4C = 6, PVD_FIT_LM_MONO = 7, PVD_FIT_LM_BI = 8, PVD_FIT_LM_TRI = 9
 };
-enum { PVD_FIT_FORCE_ZERO_AT_T0 = 1, PVD_FIT_P0_GIVEN = 2 };
+/* Flags.  PVD_FIT_P0_FROM_DATA (f4a only): start from exponential peeling of
+ * each voxel's samples instead of p0.  PVD_FIT_AUC_INF (mono, f2, f4a): the
+ * AUC is the fitted curve's integral from 0 to infinity (all rates must come out
+ * positive; otherwise the voxel is marked not ok and the model's own AUC rule is
+ * used).  PVD_FIT_MIXED runs the iterations in FP32 and finishes in FP64.
+ * None of the three exists in the reference; they serve the time-integrated dose
+ * of a whole batch of volumes.  auc_f32_d (nullable) receives
+ * float(auc * auc_f32_scale), e.g. cumulated activity in Bq s for a convolution. */
+enum {
+  PVD_FIT_FORCE_ZERO_AT_T0 = 1,
+  PVD_FIT_P0_GIVEN = 2,
+  PVD_FIT_P0_FROM_DATA = 4,
+  PVD_FIT_AUC_INF = 8,
+  PVD_FIT_MIXED = 16 /* Levenberg-Marquardt in FP32, then FP64 Gauss-Newton polish and FP64 AUC
+                        (GB300's FP64 rate is a small fraction of its FP32 rate) */
+};
 pvd_status pvd_tac_fit(int model, const double* times, const double* weights, int n_times,
                        const double* p0, double lam_phys, double auc_limit, int max_fev, int flags,
                        const float* acts_d, long long n_vox, double* params_d, double* auc_d,
-                       unsigned char* ok_d, pvd_stream stream);
+                       unsigned char* ok_d, float* auc_f32_d, double auc_f32_scale, pvd_stream stream);
 
 /* ------------------------------------------------------------------------ */
 /* Monte Carlo transport                                                      */

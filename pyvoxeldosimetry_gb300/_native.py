@@ -21,6 +21,10 @@ PVD_MODE_LINEAR = 0
 PVD_MODE_CIRCULAR = 1
 PVD_KERNEL_NORMALIZE = 1
 PVD_PLAN_TMA = 1
+PVD_FIT_P0_GIVEN = 2
+PVD_FIT_P0_FROM_DATA = 4
+PVD_FIT_AUC_INF = 8
+PVD_FIT_MIXED = 16
 PVD_MAX_KERNELS = 8
 PVD_MAX_TIMEPOINTS = 16
 
@@ -109,7 +113,7 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_fast_lengths": (i, [C.POINTER(C.c_int), i]),
         "pvd_plan_pass_times": (st, [vp, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
         "pvd_weighted_sum": (st, [vp, vp, i, C.c_longlong, vp, vp]),
-        "pvd_tac_fit": (st, [i, vp, vp, i, vp, d, d, i, i, vp, C.c_longlong, vp, vp, vp, vp]),
+        "pvd_tac_fit": (st, [i, vp, vp, i, vp, d, d, i, i, vp, C.c_longlong, vp, vp, vp, vp, d, vp]),
         "pvd_mc_plan_create": (st, [C.POINTER(McDesc), C.POINTER(vp)]),
         "pvd_mc_run": (st, [vp, vp, vp, C.c_ulonglong, C.c_ulonglong, vp, vp, C.POINTER(McStats), vp]),
         "pvd_mc_plan_destroy": (st, [vp]),

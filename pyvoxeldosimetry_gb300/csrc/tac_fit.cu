@@ -24,6 +24,8 @@
 
 namespace pvd {
 
+#define PVD_LN2 0.69314718055994530942
+
 enum Model {
   M_MONO_LAMBDA = 0,  // A0 exp(-lam t)                     (fit_time_activity_curve)
   M_F2 = 1, M_F3 = 2, M_F3A = 3, M_F4A = 4, M_F4B = 5, M_F4C = 6,  // NUKFIT
@@ -40,17 +42,42 @@ struct FitArgs {
   int max_fev;                  // model-evaluation budget (curve_fit's maxfev)
   int force_zero_at_t0;
   int p0_from_data;              // mono-lambda: p0 = [y(t0), lam_phys] per voxel
+  int p0_peel;                   // f4a: p0 from exponential peeling of the samples
+  int auc_inf;                   // f2 / f4a / mono: analytic integral to infinity
+  double f32_scale;              // scale of the optional float32 copy of the AUC
+  int mixed;                     // FP32 Levenberg-Marquardt, then FP64 Gauss-Newton polish
 };
 
-template <int M> struct ModelTraits;
+// Start for the two-exponential model f4a from "exponential peeling": the slow
+// rate from the last two samples, the fast one from what it leaves at the first
+// two.  Rates are total (physical + biological); returned params subtract lp.
+__device__ void peel_biexp(const FitArgs& a, const double* y, double* p) {
+  const int T = a.T;
+  const double t0 = a.t[0], t1 = a.t[1], tA = a.t[T - 2], tB = a.t[T - 1];
+  double k2 = PVD_LN2 / (10.0 * tB);
+  if (y[T - 2] > 0.0 && y[T - 1] > 0.0 && y[T - 2] > y[T - 1]) k2 = log(y[T - 2] / y[T - 1]) / (tB - tA);
+  const double A2 = y[T - 1] * exp(k2 * tB);
+  const double r0 = y[0] - A2 * exp(-k2 * t0), r1 = y[1] - A2 * exp(-k2 * t1);
+  double k1 = 4.0 * k2 + PVD_LN2 / t1, A1 = 0.0;
+  if (r0 > 0.0 && r1 > 0.0 && r0 > r1) {
+    const double kk = log(r0 / r1) / (t1 - t0);
+    if (kk > k2) k1 = kk;
+  }
+  if (r0 > 0.0) A1 = r0 * exp(k1 * t0);
+  p[0] = A1;
+  p[1] = k1 - a.lam_phys;
+  p[2] = A2;
+  p[3] = k2 - a.lam_phys;
+}
 
-#define PVD_LN2 0.69314718055994530942
+template <int M> struct ModelTraits;
 
 // value and gradient of each model at time t
 template <> struct ModelTraits<M_MONO_LAMBDA> {
   static constexpr int N = 2;
-  static __device__ double eval(const double* p, double t, double, double* g) {
-    const double e = exp(-p[1] * t);
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R, R* g) {
+    const R e = exp(-p[1] * t);
     g[0] = e;
     g[1] = -t * p[0] * e;
     return p[0] * e;
@@ -58,8 +85,9 @@ template <> struct ModelTraits<M_MONO_LAMBDA> {
 };
 template <> struct ModelTraits<M_F2> {
   static constexpr int N = 2;
-  static __device__ double eval(const double* p, double t, double lp, double* g) {
-    const double e = exp(-(p[1] + lp) * t);
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R lp, R* g) {
+    const R e = exp(-(p[1] + lp) * t);
     g[0] = e;
     g[1] = -t * p[0] * e;
     return p[0] * e;
@@ -67,8 +95,9 @@ template <> struct ModelTraits<M_F2> {
 };
 template <> struct ModelTraits<M_F3> {
   static constexpr int N = 3;
-  static __device__ double eval(const double* p, double t, double lp, double* g) {
-    const double e1 = exp(-(p[1] + lp) * t), e2 = exp(-(p[2] + lp) * t);
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R lp, R* g) {
+    const R e1 = exp(-(p[1] + lp) * t), e2 = exp(-(p[2] + lp) * t);
     g[0] = e1 - e2;
     g[1] = -t * p[0] * e1;
     g[2] = t * p[0] * e2;
@@ -77,18 +106,20 @@ template <> struct ModelTraits<M_F3> {
 };
 template <> struct ModelTraits<M_F3A> {
   static constexpr int N = 3;
-  static __device__ double eval(const double* p, double t, double lp, double* g) {
-    const double e1 = exp(-(p[2] + lp) * t), ep = exp(-lp * t);
-    g[0] = p[1] * e1 + (1 - p[1]) * ep;
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R lp, R* g) {
+    const R e1 = exp(-(p[2] + lp) * t), ep = exp(-lp * t);
+    g[0] = p[1] * e1 + ((R)1 - p[1]) * ep;
     g[1] = p[0] * (e1 - ep);
     g[2] = -t * p[0] * p[1] * e1;
-    return p[0] * (p[1] * e1 + (1 - p[1]) * ep);
+    return p[0] * (p[1] * e1 + ((R)1 - p[1]) * ep);
   }
 };
 template <> struct ModelTraits<M_F4A> {
   static constexpr int N = 4;
-  static __device__ double eval(const double* p, double t, double lp, double* g) {
-    const double e1 = exp(-(p[1] + lp) * t), e2 = exp(-(p[3] + lp) * t);
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R lp, R* g) {
+    const R e1 = exp(-(p[1] + lp) * t), e2 = exp(-(p[3] + lp) * t);
     g[0] = e1;
     g[1] = -t * p[0] * e1;
     g[2] = e2;
@@ -98,8 +129,9 @@ template <> struct ModelTraits<M_F4A> {
 };
 template <> struct ModelTraits<M_F4B> {
   static constexpr int N = 5;
-  static __device__ double eval(const double* p, double t, double lp, double* g) {
-    const double e1 = exp(-(p[1] + lp) * t), e2 = exp(-(p[3] + lp) * t), eb = exp(-(p[4] + lp) * t);
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R lp, R* g) {
+    const R e1 = exp(-(p[1] + lp) * t), e2 = exp(-(p[3] + lp) * t), eb = exp(-(p[4] + lp) * t);
     g[0] = e1 - eb;
     g[1] = -t * p[0] * e1;
     g[2] = -e2 + eb;
@@ -110,8 +142,9 @@ template <> struct ModelTraits<M_F4B> {
 };
 template <> struct ModelTraits<M_F4C> {
   static constexpr int N = 5;
-  static __device__ double eval(const double* p, double t, double lp, double* g) {
-    const double e1 = exp(-(p[1] + lp) * t), e2 = exp(-(p[3] + lp) * t), eb = exp(-(p[4] + lp) * t);
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R lp, R* g) {
+    const R e1 = exp(-(p[1] + lp) * t), e2 = exp(-(p[3] + lp) * t), eb = exp(-(p[4] + lp) * t);
     g[0] = e1 - eb;
     g[1] = -t * p[0] * e1;
     g[2] = e2 - eb;
@@ -122,51 +155,55 @@ template <> struct ModelTraits<M_F4C> {
 };
 template <> struct ModelTraits<M_LM_MONO> {
   static constexpr int N = 2;
-  static __device__ double eval(const double* p, double t, double, double* g) {
-    const double e = exp(-PVD_LN2 * t / p[1]);
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R, R* g) {
+    const R e = exp(-(R)PVD_LN2 * t / p[1]);
     g[0] = e;
-    g[1] = p[0] * e * PVD_LN2 * t / (p[1] * p[1]);
+    g[1] = p[0] * e * (R)PVD_LN2 * t / (p[1] * p[1]);
     return p[0] * e;
   }
 };
 template <> struct ModelTraits<M_LM_BI> {
   static constexpr int N = 3;
-  static __device__ double eval(const double* p, double t, double, double* g) {
-    const double e1 = exp(-PVD_LN2 * t / p[1]), e2 = exp(-PVD_LN2 * t / p[2]);
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R, R* g) {
+    const R e1 = exp(-(R)PVD_LN2 * t / p[1]), e2 = exp(-(R)PVD_LN2 * t / p[2]);
     g[0] = e1 - e2;
-    g[1] = p[0] * e1 * PVD_LN2 * t / (p[1] * p[1]);
-    g[2] = -p[0] * e2 * PVD_LN2 * t / (p[2] * p[2]);
+    g[1] = p[0] * e1 * (R)PVD_LN2 * t / (p[1] * p[1]);
+    g[2] = -p[0] * e2 * (R)PVD_LN2 * t / (p[2] * p[2]);
     return p[0] * (e1 - e2);
   }
 };
 template <> struct ModelTraits<M_LM_TRI> {
   static constexpr int N = 5;
-  static __device__ double eval(const double* p, double t, double, double* g) {
-    const double e1 = exp(-PVD_LN2 * t / p[1]), e2 = exp(-PVD_LN2 * t / p[3]), e3 = exp(-PVD_LN2 * t / p[4]);
+  template <typename R>
+  static __device__ R eval(const R* p, R t, R, R* g) {
+    const R e1 = exp(-(R)PVD_LN2 * t / p[1]), e2 = exp(-(R)PVD_LN2 * t / p[3]), e3 = exp(-(R)PVD_LN2 * t / p[4]);
     g[0] = e1 - e3;
-    g[1] = p[0] * e1 * PVD_LN2 * t / (p[1] * p[1]);
+    g[1] = p[0] * e1 * (R)PVD_LN2 * t / (p[1] * p[1]);
     g[2] = -e2 + e3;
-    g[3] = -p[2] * e2 * PVD_LN2 * t / (p[3] * p[3]);
-    g[4] = -(p[0] - p[2]) * e3 * PVD_LN2 * t / (p[4] * p[4]);
+    g[3] = -p[2] * e2 * (R)PVD_LN2 * t / (p[3] * p[3]);
+    g[4] = -(p[0] - p[2]) * e3 * (R)PVD_LN2 * t / (p[4] * p[4]);
     return p[0] * e1 - p[2] * e2 - (p[0] - p[2]) * e3;
   }
 };
 
 // normal equations at p: A = J^T J (upper triangle), g = J^T r, returns 0.5 r^T r
-template <int M>
-__device__ double normal_eq(const FitArgs& a, const double* y, const double* p, double* A, double* g) {
+template <int M, typename R>
+__device__ R normal_eq(const FitArgs& a, const R* y, const R* p, R* A, R* g) {
   constexpr int N = ModelTraits<M>::N;
 #pragma unroll
-  for (int i = 0; i < N * N; ++i) A[i] = 0.0;
+  for (int i = 0; i < N * N; ++i) A[i] = (R)0;
 #pragma unroll
-  for (int i = 0; i < N; ++i) g[i] = 0.0;
-  double cost = 0.0;
+  for (int i = 0; i < N; ++i) g[i] = (R)0;
+  R cost = (R)0;
   for (int k = 0; k < a.T; ++k) {
-    double j[N];
-    const double f = ModelTraits<M>::eval(p, a.t[k], a.lam_phys, j);
-    const double r = a.w[k] * (f - y[k]);
+    R j[N];
+    const R w = (R)a.w[k];
+    const R f = ModelTraits<M>::template eval<R>(p, (R)a.t[k], (R)a.lam_phys, j);
+    const R r = w * (f - y[k]);
 #pragma unroll
-    for (int i = 0; i < N; ++i) j[i] *= a.w[k];
+    for (int i = 0; i < N; ++i) j[i] *= w;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       g[i] += j[i] * r;
@@ -175,33 +212,47 @@ __device__ double normal_eq(const FitArgs& a, const double* y, const double* p, 
     }
     cost += r * r;
   }
-  return 0.5 * cost;
+  return (R)0.5 * cost;
 }
 
-template <int M>
-__device__ double cost_at(const FitArgs& a, const double* y, const double* p) {
+template <int M, typename R>
+__device__ R cost_at(const FitArgs& a, const R* y, const R* p) {
   constexpr int N = ModelTraits<M>::N;
-  double cost = 0.0;
+  R cost = (R)0;
   for (int k = 0; k < a.T; ++k) {
-    double j[N];
-    const double r = a.w[k] * (ModelTraits<M>::eval(p, a.t[k], a.lam_phys, j) - y[k]);
+    R j[N];
+    const R r = (R)a.w[k] * (ModelTraits<M>::template eval<R>(p, (R)a.t[k], (R)a.lam_phys, j) - y[k]);
     cost += r * r;
   }
-  return 0.5 * cost;
+  return (R)0.5 * cost;
 }
+
+// tolerances per precision: MINPACK's defaults (sqrt(eps) ftol/xtol) in double; the
+// float iterations stop at 1e-6 and are followed by a double polish
+template <typename R> struct Lim;
+template <> struct Lim<double> {
+  static __device__ double tiny() { return 2.2250738585072014e-308; }
+  static __device__ double tol() { return 1.49012e-8; }
+  static __device__ double eps() { return 2.220446049250313e-16; }
+};
+template <> struct Lim<float> {
+  static __device__ float tiny() { return 1.17549435e-38f; }
+  static __device__ float tol() { return 1e-6f; }
+  static __device__ float eps() { return 1.1920929e-7f; }
+};
 
 // Cholesky of (A + par diag(D^2)) (A symmetric, upper triangle stored in A[i*N+c], c >= i).
 // L is lower triangular, row major.  false if not positive definite.
-template <int N>
-__device__ bool chol_damped(const double* A, const double* D, double par, double* L) {
+template <int N, typename R>
+__device__ bool chol_damped(const R* A, const R* D, R par, R* L) {
 #pragma unroll
   for (int i = 0; i < N; ++i) {
 #pragma unroll
     for (int c = 0; c <= i; ++c) {
-      double s = (c == i) ? A[i * N + i] + par * D[i] * D[i] : A[c * N + i];
+      R s = (c == i) ? A[i * N + i] + par * D[i] * D[i] : A[c * N + i];
       for (int k = 0; k < c; ++k) s -= L[i * N + k] * L[c * N + k];
       if (c == i) {
-        if (!(s > 0.0)) return false;
+        if (!(s > (R)0.0)) return false;
         L[i * N + i] = sqrt(s);
       } else {
         L[i * N + c] = s / L[c * N + c];
@@ -211,34 +262,34 @@ __device__ bool chol_damped(const double* A, const double* D, double par, double
   return true;
 }
 
-template <int N>
-__device__ void chol_fwd(const double* L, const double* b, double* z) {  // L z = b
+template <int N, typename R>
+__device__ void chol_fwd(const R* L, const R* b, R* z) {  // L z = b
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    double s = b[i];
+    R s = b[i];
     for (int k = 0; k < i; ++k) s -= L[i * N + k] * z[k];
     z[i] = s / L[i * N + i];
   }
 }
 
-template <int N>
-__device__ void chol_solve_neg(const double* L, const double* g, double* p) {  // L L^T p = -g
-  double z[N];
-  double mg[N];
+template <int N, typename R>
+__device__ void chol_solve_neg(const R* L, const R* g, R* p) {  // L L^T p = -g
+  R z[N];
+  R mg[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) mg[i] = -g[i];
-  chol_fwd<N>(L, mg, z);
+  chol_fwd<N, R>(L, mg, z);
 #pragma unroll
   for (int i = N - 1; i >= 0; --i) {
-    double s = z[i];
+    R s = z[i];
     for (int k = i + 1; k < N; ++k) s -= L[k * N + i] * p[k];
     p[i] = s / L[i * N + i];
   }
 }
 
-template <int N>
-__device__ double dnorm(const double* D, const double* v) {
-  double s = 0.0;
+template <int N, typename R>
+__device__ R dnorm(const R* D, const R* v) {
+  R s = (R)0.0;
 #pragma unroll
   for (int i = 0; i < N; ++i) s += (D[i] * v[i]) * (D[i] * v[i]);
   return sqrt(s);
@@ -248,58 +299,58 @@ __device__ double dnorm(const double* D, const double* v) {
 // and theory", 1978, the lmpar procedure) on the normal equations: find
 // par >= 0 with ||D p|| within 10 % of delta, p = -(A + par D^2)^-1 g, or the
 // Gauss-Newton step (par = 0) when it already fits in the region.
-template <int N>
-__device__ void lm_par(const double* A, const double* g, const double* D, double delta, double& par, double* p) {
-  const double dwarf = 2.2250738585072014e-308;
-  double L[N * N], w[N], q[N];
-  double parl = 0.0;
-  double fp;
-  if (chol_damped<N>(A, D, 0.0, L)) {
-    chol_solve_neg<N>(L, g, p);
-    const double dxn = dnorm<N>(D, p);
+template <int N, typename R>
+__device__ void lm_par(const R* A, const R* g, const R* D, R delta, R& par, R* p) {
+  const R dwarf = Lim<R>::tiny();
+  R L[N * N], w[N], q[N];
+  R parl = (R)0.0;
+  R fp;
+  if (chol_damped<N, R>(A, D, (R)0.0, L)) {
+    chol_solve_neg<N, R>(L, g, p);
+    const R dxn = dnorm<N, R>(D, p);
     fp = dxn - delta;
-    if (fp <= 0.1 * delta) {
-      par = 0.0;
+    if (fp <= (R)0.1 * delta) {
+      par = (R)0.0;
       return;
     }
 #pragma unroll
     for (int i = 0; i < N; ++i) q[i] = D[i] * (D[i] * p[i]) / dxn;
-    chol_fwd<N>(L, q, w);
-    double wn = 0.0;
+    chol_fwd<N, R>(L, q, w);
+    R wn = (R)0.0;
 #pragma unroll
     for (int i = 0; i < N; ++i) wn += w[i] * w[i];
     parl = (fp / delta) / wn;
   }
-  double gn = 0.0;
+  R gn = (R)0.0;
 #pragma unroll
   for (int i = 0; i < N; ++i) gn += (g[i] / D[i]) * (g[i] / D[i]);
   gn = sqrt(gn);
-  double paru = gn / delta;
-  if (paru == 0.0) paru = dwarf / fmin(delta, 0.1);
+  R paru = gn / delta;
+  if (paru == (R)0.0) paru = dwarf / fmin(delta, (R)0.1);
   par = fmax(par, parl);
   par = fmin(par, paru);
-  if (par == 0.0) par = gn / fmax(dnorm<N>(D, p), dwarf);
-  fp = 0.0;
+  if (par == (R)0.0) par = gn / fmax(dnorm<N, R>(D, p), dwarf);
+  fp = (R)0.0;
   for (int it = 1; it <= 10; ++it) {
-    if (par == 0.0) par = fmax(dwarf, 0.001 * paru);
-    if (!chol_damped<N>(A, D, par, L)) {  // only possible when D has zero entries
-      par = fmax(par * 10.0, dwarf);
+    if (par == (R)0.0) par = fmax(dwarf, (R)0.001 * paru);
+    if (!chol_damped<N, R>(A, D, par, L)) {  // only possible when D has zero entries
+      par = fmax(par * (R)10.0, dwarf);
       continue;
     }
-    chol_solve_neg<N>(L, g, p);
-    const double dxn = dnorm<N>(D, p);
-    const double temp = fp;
+    chol_solve_neg<N, R>(L, g, p);
+    const R dxn = dnorm<N, R>(D, p);
+    const R temp = fp;
     fp = dxn - delta;
-    if (fabs(fp) <= 0.1 * delta || (parl == 0.0 && fp <= temp && temp < 0.0) || it == 10) break;
+    if (fabs(fp) <= (R)0.1 * delta || (parl == (R)0.0 && fp <= temp && temp < (R)0.0) || it == 10) break;
 #pragma unroll
     for (int i = 0; i < N; ++i) q[i] = D[i] * (D[i] * p[i]) / dxn;
-    chol_fwd<N>(L, q, w);
-    double wn = 0.0;
+    chol_fwd<N, R>(L, q, w);
+    R wn = (R)0.0;
 #pragma unroll
     for (int i = 0; i < N; ++i) wn += w[i] * w[i];
-    const double parc = (fp / delta) / wn;
-    if (fp > 0.0) parl = fmax(parl, par);
-    if (fp < 0.0) paru = fmin(paru, par);
+    const R parc = (fp / delta) / wn;
+    if (fp > (R)0.0) parl = fmax(parl, par);
+    if (fp < (R)0.0) paru = fmin(paru, par);
     par = fmax(parl, par + parc);
   }
 }
@@ -309,92 +360,121 @@ __device__ void lm_par(const double* A, const double* g, const double* D, double
 // both / gtol), 5 evaluation budget exhausted, 6-8 tolerances too small, -1
 // non-finite cost.  `maxfev` counts model evaluations as a forward-difference
 // Jacobian would (N per Jacobian), so the budget matches curve_fit's.
-template <int M>
-__device__ int lm_fit(const FitArgs& a, const double* y, double* x, int maxfev) {
+template <int M, typename R>
+__device__ int lm_fit(const FitArgs& a, const R* y, R* x, int maxfev) {
   constexpr int N = ModelTraits<M>::N;
-  const double ftol = 1.49012e-8, xtol = 1.49012e-8, epsmch = 2.220446049250313e-16;
-  double A[N * N], g[N], D[N], p[N], xt[N];
+  const R ftol = Lim<R>::tol(), xtol = Lim<R>::tol(), epsmch = Lim<R>::eps();
+  R A[N * N], g[N], D[N], p[N], xt[N];
   int nfev = 1;
-  double fnorm = sqrt(2.0 * cost_at<M>(a, y, x));
+  R fnorm = sqrt((R)2.0 * cost_at<M, R>(a, y, x));
   if (!isfinite(fnorm)) return -1;
-  double delta = 0.0, xnorm = 0.0, par = 0.0;
+  R delta = (R)0.0, xnorm = (R)0.0, par = (R)0.0;
   for (int iter = 1;; ++iter) {
-    normal_eq<M>(a, y, x, A, g);
+    normal_eq<M, R>(a, y, x, A, g);
     nfev += N;
-    double acn[N];
+    R acn[N];
 #pragma unroll
     for (int j = 0; j < N; ++j) acn[j] = sqrt(A[j * N + j]);
     if (iter == 1) {
 #pragma unroll
-      for (int j = 0; j < N; ++j) D[j] = (acn[j] == 0.0) ? 1.0 : acn[j];
-      xnorm = dnorm<N>(D, x);
-      delta = 100.0 * xnorm;
-      if (delta == 0.0) delta = 100.0;
+      for (int j = 0; j < N; ++j) D[j] = (acn[j] == (R)0.0) ? (R)1.0 : acn[j];
+      xnorm = dnorm<N, R>(D, x);
+      delta = (R)100.0 * xnorm;
+      if (delta == (R)0.0) delta = (R)100.0;
     }
-    double gnorm = 0.0;
-    if (fnorm != 0.0) {
+    R gnorm = (R)0.0;
+    if (fnorm != (R)0.0) {
 #pragma unroll
       for (int j = 0; j < N; ++j)
-        if (acn[j] != 0.0) gnorm = fmax(gnorm, fabs(g[j] / fnorm) / acn[j]);
+        if (acn[j] != (R)0.0) gnorm = fmax(gnorm, fabs(g[j] / fnorm) / acn[j]);
     }
-    if (gnorm <= 0.0) return 4;  // gtol = 0
+    if (gnorm <= (R)0.0) return 4;  // gtol = 0
 #pragma unroll
     for (int j = 0; j < N; ++j) D[j] = fmax(D[j], acn[j]);
-    double ratio = 0.0;
+    R ratio = (R)0.0;
     do {
-      lm_par<N>(A, g, D, delta, par, p);
+      lm_par<N, R>(A, g, D, delta, par, p);
 #pragma unroll
       for (int j = 0; j < N; ++j) xt[j] = x[j] + p[j];
-      const double pnorm = dnorm<N>(D, p);
+      const R pnorm = dnorm<N, R>(D, p);
       if (iter == 1) delta = fmin(delta, pnorm);
-      const double fnorm1 = sqrt(2.0 * cost_at<M>(a, y, xt));
+      const R fnorm1 = sqrt((R)2.0 * cost_at<M, R>(a, y, xt));
       nfev += 1;
-      double actred = -1.0;
-      if (0.1 * fnorm1 < fnorm) actred = 1.0 - (fnorm1 / fnorm) * (fnorm1 / fnorm);
-      double jp2 = 0.0;  // ||J p||^2 = p^T A p
+      R actred = -(R)1.0;
+      if ((R)0.1 * fnorm1 < fnorm) actred = (R)1.0 - (fnorm1 / fnorm) * (fnorm1 / fnorm);
+      R jp2 = (R)0.0;  // ||J p||^2 = p^T A p
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        double row = 0.0;
+        R row = (R)0.0;
 #pragma unroll
         for (int c = 0; c < N; ++c) row += (c >= i ? A[i * N + c] : A[c * N + i]) * p[c];
         jp2 += p[i] * row;
       }
-      const double t1 = sqrt(fmax(jp2, 0.0)) / fnorm;
-      const double t2 = sqrt(par) * pnorm / fnorm;
-      const double prered = t1 * t1 + t2 * t2 / 0.5;
-      const double dirder = -(t1 * t1 + t2 * t2);
-      ratio = (prered != 0.0) ? actred / prered : 0.0;
-      if (!isfinite(fnorm1)) ratio = 0.0;
-      if (ratio <= 0.25) {
-        double temp = (actred >= 0.0) ? 0.5 : 0.5 * dirder / (dirder + 0.5 * actred);
-        if (0.1 * fnorm1 >= fnorm || temp < 0.1 || !isfinite(fnorm1)) temp = 0.1;
-        delta = temp * fmin(delta, pnorm / 0.1);
+      const R t1 = sqrt(fmax(jp2, (R)0.0)) / fnorm;
+      const R t2 = sqrt(par) * pnorm / fnorm;
+      const R prered = t1 * t1 + t2 * t2 / (R)0.5;
+      const R dirder = -(t1 * t1 + t2 * t2);
+      ratio = (prered != (R)0.0) ? actred / prered : (R)0.0;
+      if (!isfinite(fnorm1)) ratio = (R)0.0;
+      if (ratio <= (R)0.25) {
+        R temp = (actred >= (R)0.0) ? (R)0.5 : (R)0.5 * dirder / (dirder + (R)0.5 * actred);
+        if ((R)0.1 * fnorm1 >= fnorm || temp < (R)0.1 || !isfinite(fnorm1)) temp = (R)0.1;
+        delta = temp * fmin(delta, pnorm / (R)0.1);
         par = par / temp;
-      } else if (par == 0.0 || ratio >= 0.75) {
-        delta = pnorm / 0.5;
-        par = 0.5 * par;
+      } else if (par == (R)0.0 || ratio >= (R)0.75) {
+        delta = pnorm / (R)0.5;
+        par = (R)0.5 * par;
       }
-      if (ratio >= 1e-4) {
+      if (ratio >= (R)1e-4) {
 #pragma unroll
         for (int j = 0; j < N; ++j) x[j] = xt[j];
         fnorm = fnorm1;
-        xnorm = dnorm<N>(D, x);
+        xnorm = dnorm<N, R>(D, x);
       }
       int info = 0;
-      if (fabs(actred) <= ftol && prered <= ftol && 0.5 * ratio <= 1.0) info = 1;
+      if (fabs(actred) <= ftol && prered <= ftol && (R)0.5 * ratio <= (R)1.0) info = 1;
       if (delta <= xtol * xnorm) info = (info == 1) ? 3 : 2;
       if (info) return info;
       if (nfev >= maxfev) return 5;
-      if (fabs(actred) <= epsmch && prered <= epsmch && 0.5 * ratio <= 1.0) return 6;
+      if (fabs(actred) <= epsmch && prered <= epsmch && (R)0.5 * ratio <= (R)1.0) return 6;
       if (delta <= epsmch * xnorm) return 7;
       if (gnorm <= epsmch) return 8;
-    } while (ratio < 1e-4);
+    } while (ratio < (R)1e-4);
   }
+}
+
+// FP64 Gauss-Newton refinement of an FP32 least-squares solution: a few
+// normal-equation steps, each kept only if it lowers the FP64 cost.  False if
+// the cost is not finite.
+template <int M>
+__device__ bool polish_fp64(const FitArgs& a, const double* y, double* p) {
+  constexpr int N = ModelTraits<M>::N;
+  double A[N * N], g[N], L[N * N], h[N], pn[N], D[N];
+  for (int it = 0; it < 4; ++it) {
+    const double F = normal_eq<M, double>(a, y, p, A, g);
+    if (!isfinite(F)) return false;
+    if (F == 0.0) return true;
+    double dmax = 0.0;
+#pragma unroll
+    for (int i = 0; i < N; ++i) dmax = fmax(dmax, A[i * N + i]);
+#pragma unroll
+    for (int i = 0; i < N; ++i) D[i] = 1.0;
+    if (!chol_damped<N, double>(A, D, 1e-14 * dmax, L)) return true;
+    chol_solve_neg<N, double>(L, g, h);
+#pragma unroll
+    for (int i = 0; i < N; ++i) pn[i] = p[i] + h[i];
+    const double Fn = cost_at<M, double>(a, y, pn);
+    if (!(Fn < F)) return true;
+#pragma unroll
+    for (int i = 0; i < N; ++i) p[i] = pn[i];
+    if (F - Fn <= 1e-15 * F) return true;
+  }
+  return true;
 }
 
 template <int M>
 __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long nvox, double* __restrict__ params,
-                          double* __restrict__ auc, unsigned char* __restrict__ ok) {
+                          double* __restrict__ auc, unsigned char* __restrict__ ok, float* __restrict__ auc32) {
   constexpr int N = ModelTraits<M>::N;
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvox; v += (long long)gridDim.x * blockDim.x) {
     double y[PVD_MAX_TIMEPOINTS];
@@ -415,8 +495,25 @@ __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long n
       p[0] = y[0];
       p[1] = a.lam_phys;
     }
-    const int info = (finite && a.T >= N) ? lm_fit<M>(a, y, p, a.max_fev) : -1;
-    const bool good = info >= 1 && info <= 4;  // curve_fit raises for any other outcome
+    if constexpr (M == M_F4A) {
+      if (a.p0_peel && finite && a.T >= 4) peel_biexp(a, y, p);
+    }
+    int info = -1;
+    if (!(finite && a.T >= N)) {
+      info = -1;
+    } else if (a.mixed) {
+      float yf[PVD_MAX_TIMEPOINTS], pf[N];
+      for (int k = 0; k < a.T; ++k) yf[k] = (float)y[k];
+#pragma unroll
+      for (int i = 0; i < N; ++i) pf[i] = (float)p[i];
+      info = lm_fit<M, float>(a, yf, pf, a.max_fev);
+#pragma unroll
+      for (int i = 0; i < N; ++i) p[i] = (double)pf[i];
+      if (info != 5 && info != -1) info = polish_fp64<M>(a, y, p) ? 1 : 5;
+    } else {
+      info = lm_fit<M, double>(a, y, p, a.max_fev);
+    }
+    bool good = info >= 1 && info <= 4;  // curve_fit raises for any other outcome
     if (!good) {
       if (M == M_MONO_LAMBDA) {  // fallback [0, lam_phys] (curve_fitting.py:58-59)
         p[0] = 0.0;
@@ -428,22 +525,46 @@ __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long n
     }
 #pragma unroll
     for (int i = 0; i < N; ++i) params[(long long)i * nvox + v] = p[i];
-    double s;
-    if (M == M_MONO_LAMBDA) {
+    double s = 0.0;
+    bool inf_done = false;
+    if (a.auc_inf && good) {  // integral of the fitted curve from 0 to infinity
+      if constexpr (M == M_MONO_LAMBDA) {
+        if (p[1] > 0.0) {
+          s = p[0] / p[1];
+          inf_done = true;
+        }
+      } else if constexpr (M == M_F2) {
+        const double k = p[1] + a.lam_phys;
+        if (k > 0.0) {
+          s = p[0] / k;
+          inf_done = true;
+        }
+      } else if constexpr (M == M_F4A) {
+        const double k1 = p[1] + a.lam_phys, k2 = p[3] + a.lam_phys;
+        if (k1 > 0.0 && k2 > 0.0) {
+          s = p[0] / k1 + p[2] / k2;
+          inf_done = true;
+        }
+      }
+      if (!inf_done) good = false;  // diverging or unsupported: the sampled-interval rule below
+    }
+    if (inf_done) {
+    } else if (M == M_MONO_LAMBDA) {
       // A0 / lam * (1 - exp(-lam * limit))  (curve_fitting.py:74-84)
       s = p[0] / p[1] * (1.0 - exp(-p[1] * a.auc_limit));
     } else {
       // trapezoid of the fitted curve over the sampled times (curve_fitting.py:215)
       double j[N];
       s = 0.0;
-      double fprev = ModelTraits<M>::eval(p, a.t[0], a.lam_phys, j);
+      double fprev = ModelTraits<M>::template eval<double>(p, a.t[0], a.lam_phys, j);
       for (int k = 1; k < a.T; ++k) {
-        const double f = ModelTraits<M>::eval(p, a.t[k], a.lam_phys, j);
+        const double f = ModelTraits<M>::template eval<double>(p, a.t[k], a.lam_phys, j);
         s += 0.5 * (f + fprev) * (a.t[k] - a.t[k - 1]);
         fprev = f;
       }
     }
     auc[v] = s;
+    if (auc32) auc32[v] = (float)(s * a.f32_scale);
     if (ok) ok[v] = good ? 1 : 0;
   }
 }
@@ -455,7 +576,7 @@ using namespace pvd;
 extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* weights, int n_times,
                                   const double* p0, double lam_phys, double auc_limit, int max_fev, int flags,
                                   const float* acts_d, long long n_vox, double* params_d, double* auc_d,
-                                  unsigned char* ok_d, pvd_stream stream) {
+                                  unsigned char* ok_d, float* auc_f32_d, double auc_f32_scale, pvd_stream stream) {
   if (!times || !acts_d || !params_d || !auc_d) return set_error(PVD_ERR_ARG, "pvd_tac_fit: null argument");
   if (n_times < 1 || n_times > PVD_MAX_TIMEPOINTS) return set_error(PVD_ERR_ARG, "pvd_tac_fit: n_times must be in [1, 16]");
   if (n_vox < 0) return set_error(PVD_ERR_ARG, "pvd_tac_fit: negative voxel count");
@@ -475,13 +596,21 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
   a.max_fev = max_fev;
   a.force_zero_at_t0 = (flags & PVD_FIT_FORCE_ZERO_AT_T0) ? 1 : 0;
   a.p0_from_data = (model == M_MONO_LAMBDA && !(flags & PVD_FIT_P0_GIVEN)) ? 1 : 0;
+  a.p0_peel = (flags & PVD_FIT_P0_FROM_DATA) ? 1 : 0;
+  a.auc_inf = (flags & PVD_FIT_AUC_INF) ? 1 : 0;
+  a.f32_scale = auc_f32_scale;
+  a.mixed = (flags & PVD_FIT_MIXED) ? 1 : 0;
+  if ((flags & PVD_FIT_P0_FROM_DATA) && model != M_F4A)
+    return set_error(PVD_ERR_ARG, "pvd_tac_fit: PVD_FIT_P0_FROM_DATA applies to PVD_FIT_F4A");
+  if ((flags & PVD_FIT_AUC_INF) && model != M_MONO_LAMBDA && model != M_F2 && model != M_F4A)
+    return set_error(PVD_ERR_ARG, "pvd_tac_fit: PVD_FIT_AUC_INF applies to the mono, f2 and f4a models");
   cudaStream_t st = (cudaStream_t)stream;
   const int threads = 128;
   const int blocks = (int)std::min<long long>((n_vox + threads - 1) / threads, 152LL * 64);
   switch (model) {
 #define PVD_FIT_CASE(M)                                                                    \
   case M:                                                                                  \
-    k_tac_fit<M><<<blocks, threads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d);    \
+    k_tac_fit<M><<<blocks, threads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d); \
     break;
     PVD_FIT_CASE(M_MONO_LAMBDA)
     PVD_FIT_CASE(M_F2)

@@ -65,7 +65,7 @@ def _run_fit(model_id, n_par, times, weights, p0, lam_phys, auc_limit, max_fev, 
         w = (C.c_double * n_t)(*[float(x) for x in weights]) if weights is not None else None
         p = (C.c_double * 5)(*(list(p0) + [0.0] * (5 - len(p0)))) if p0 is not None else None
         N.check(lib.pvd_tac_fit(model_id, t, w, n_t, p, float(lam_phys), float(auc_limit), int(max_fev), flags,
-                                a.data_ptr(), nvox, params.data_ptr(), auc.data_ptr(), ok.data_ptr(),
+                                a.data_ptr(), nvox, params.data_ptr(), auc.data_ptr(), ok.data_ptr(), None, 1.0,
                                 _stream_handle(None)))
         params = params.reshape((n_par, *shape))
         auc = auc.reshape(shape)
