@@ -230,18 +230,26 @@ enum {
 /* Flags.  PVD_FIT_P0_FROM_DATA (f4a only): start from exponential peeling of
  * each voxel's samples instead of p0.  PVD_FIT_AUC_INF (mono, f2, f4a): the
  * AUC is the fitted curve's integral from 0 to infinity (all rates must come out
- * positive; otherwise the voxel is marked not ok and the model's own AUC rule is
- * used).  PVD_FIT_MIXED runs the iterations in FP32 and finishes in FP64.
- * None of the three exists in the reference; they serve the time-integrated dose
+ * positive, the f4a curve non-negative on [0, inf) and at t = 0 at most 100
+ * times the largest sample, and the integral finite;
+ * otherwise the voxel is marked not ok and the model's own AUC rule is used).  PVD_FIT_MIXED runs the iterations in FP32, then the same minimiser
+ * again in FP64 from where they stopped; success is decided by the FP64 run's
+ * convergence tests alone.  PVD_FIT_VARPRO (f4a only) minimises the same
+ * least-squares cost by variable projection: the two amplitudes are solved
+ * linearly for given rates and the trust-region iteration runs over the two
+ * rates only, which converges where the four-parameter iteration stalls in the
+ * valley of nearly equal rates; params are ordered fast rate first.
+ * None of these exists in the reference; they serve the time-integrated dose
  * of a whole batch of volumes.  auc_f32_d (nullable) receives
- * float(auc * auc_f32_scale), e.g. cumulated activity in Bq s for a convolution. */
+ * float(auc * auc_f32_scale), e.g. cumulated activity in Bq s for a convolution;
+ * a value that is not finite in float32 is stored as 0 with the voxel not ok. */
 enum {
   PVD_FIT_FORCE_ZERO_AT_T0 = 1,
   PVD_FIT_P0_GIVEN = 2,
   PVD_FIT_P0_FROM_DATA = 4,
   PVD_FIT_AUC_INF = 8,
-  PVD_FIT_MIXED = 16 /* Levenberg-Marquardt in FP32, then FP64 Gauss-Newton polish and FP64 AUC
-                        (GB300's FP64 rate is a small fraction of its FP32 rate) */
+  PVD_FIT_MIXED = 16, /* FP32 iterations, FP64 finish (GB300's FP64 rate is a small fraction of FP32's) */
+  PVD_FIT_VARPRO = 32
 };
 pvd_status pvd_tac_fit(int model, const double* times, const double* weights, int n_times,
                        const double* p0, double lam_phys, double auc_limit, int max_fev, int flags,

@@ -21,10 +21,14 @@ PVD_MODE_LINEAR = 0
 PVD_MODE_CIRCULAR = 1
 PVD_KERNEL_NORMALIZE = 1
 PVD_PLAN_TMA = 1
+(PVD_FIT_MONO_LAMBDA, PVD_FIT_F2, PVD_FIT_F3, PVD_FIT_F3A, PVD_FIT_F4A, PVD_FIT_F4B, PVD_FIT_F4C,
+ PVD_FIT_LM_MONO, PVD_FIT_LM_BI, PVD_FIT_LM_TRI) = range(10)
+PVD_FIT_FORCE_ZERO_AT_T0 = 1
 PVD_FIT_P0_GIVEN = 2
 PVD_FIT_P0_FROM_DATA = 4
 PVD_FIT_AUC_INF = 8
 PVD_FIT_MIXED = 16
+PVD_FIT_VARPRO = 32
 PVD_MAX_KERNELS = 8
 PVD_MAX_TIMEPOINTS = 16
 

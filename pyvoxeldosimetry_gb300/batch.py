@@ -1,10 +1,11 @@
 """Time-integrated dose of a batch of volumes of uneven sizes in one graph launch.
 
 For every volume (T timepoint activity maps, their times in hours, voxel size,
-optional density): a per-voxel two-exponential fit in FP64 precision
-(``pvd_tac_fit``, f4a model with exponential-peeling start; by default FP32
-Levenberg-Marquardt iterations polished in FP64), its analytic integral to
-infinity as cumulated activity, and the dose-point-kernel convolution of that
+optional density): a per-voxel two-exponential least-squares fit
+(``pvd_tac_fit``, f4a model by variable projection from an exponential-peeling
+start; by default FP32 trust-region iterations finished by FP64 ones, whose
+convergence tests decide success), its analytic integral to infinity as
+cumulated activity, and the dose-point-kernel convolution of that
 cumulated activity (``pvd_conv_execute``; density-scaled when a density map is
 given), giving absorbed dose in Gy.  ``prepare`` builds one convolution plan per
 distinct (shape, voxel size), allocates every buffer, and captures all the
@@ -106,7 +107,8 @@ class BatchDoseCalculator:
                 self._launch_all()
 
     def _launch_all(self) -> None:
-        flags = N.PVD_FIT_P0_FROM_DATA | N.PVD_FIT_AUC_INF | (N.PVD_FIT_MIXED if self.mixed_fit else 0)
+        flags = (N.PVD_FIT_P0_FROM_DATA | N.PVD_FIT_AUC_INF | N.PVD_FIT_VARPRO
+                 | (N.PVD_FIT_MIXED if self.mixed_fit else 0))
         p0 = (C.c_double * 5)(1.0, 0.1, 0.5, 0.01, 0.0)
         sh = torch.cuda.current_stream(self.device).cuda_stream
         for it in self._items:

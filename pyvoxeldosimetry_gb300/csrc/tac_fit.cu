@@ -45,19 +45,20 @@ struct FitArgs {
   int p0_peel;                   // f4a: p0 from exponential peeling of the samples
   int auc_inf;                   // f2 / f4a / mono: analytic integral to infinity
   double f32_scale;              // scale of the optional float32 copy of the AUC
-  int mixed;                     // FP32 Levenberg-Marquardt, then FP64 Gauss-Newton polish
+  int mixed;                     // FP32 Levenberg-Marquardt, then FP64 from its end point
 };
 
 // Start for the two-exponential model f4a from "exponential peeling": the slow
-// rate from the last two samples, the fast one from what it leaves at the first
-// two.  Rates are total (physical + biological); returned params subtract lp.
-__device__ void peel_biexp(const FitArgs& a, const double* y, double* p) {
-  const int T = a.T;
-  const double t0 = a.t[0], t1 = a.t[1], tA = a.t[T - 2], tB = a.t[T - 1];
+// rate from the last two samples (yA at tA, yB at tB), the fast one from what it
+// leaves at the first two.  Rates are total (physical + biological); returned
+// params subtract lp.
+__device__ void peel_biexp4(const FitArgs& a, double y0, double y1, double yA, double yB, double tA, double tB,
+                            double* p) {
+  const double t0 = a.t[0], t1 = a.t[1];
   double k2 = PVD_LN2 / (10.0 * tB);
-  if (y[T - 2] > 0.0 && y[T - 1] > 0.0 && y[T - 2] > y[T - 1]) k2 = log(y[T - 2] / y[T - 1]) / (tB - tA);
-  const double A2 = y[T - 1] * exp(k2 * tB);
-  const double r0 = y[0] - A2 * exp(-k2 * t0), r1 = y[1] - A2 * exp(-k2 * t1);
+  if (yA > 0.0 && yB > 0.0 && yA > yB) k2 = log(yA / yB) / (tB - tA);
+  const double A2 = yB * exp(k2 * tB);
+  const double r0 = y0 - A2 * exp(-k2 * t0), r1 = y1 - A2 * exp(-k2 * t1);
   double k1 = 4.0 * k2 + PVD_LN2 / t1, A1 = 0.0;
   if (r0 > 0.0 && r1 > 0.0 && r0 > r1) {
     const double kk = log(r0 / r1) / (t1 - t0);
@@ -68,6 +69,11 @@ __device__ void peel_biexp(const FitArgs& a, const double* y, double* p) {
   p[1] = k1 - a.lam_phys;
   p[2] = A2;
   p[3] = k2 - a.lam_phys;
+}
+
+__device__ void peel_biexp(const FitArgs& a, const double* y, double* p) {
+  const int T = a.T;
+  peel_biexp4(a, y[0], y[1], y[T - 2], y[T - 1], a.t[T - 2], a.t[T - 1], p);
 }
 
 template <int M> struct ModelTraits;
@@ -188,9 +194,167 @@ template <> struct ModelTraits<M_LM_TRI> {
   }
 };
 
+// tolerances per precision: MINPACK's defaults (sqrt(eps) ftol/xtol) in double; the
+// float iterations stop at 1e-6 and are followed by double ones
+template <typename R> struct Lim;
+template <> struct Lim<double> {
+  static __device__ double tiny() { return 2.2250738585072014e-308; }
+  static __device__ double tol() { return 1.49012e-8; }
+  static __device__ double eps() { return 2.220446049250313e-16; }
+};
+template <> struct Lim<float> {
+  static __device__ float tiny() { return 1.17549435e-38f; }
+  static __device__ float tol() { return 1e-6f; }
+  static __device__ float eps() { return 1.1920929e-7f; }
+};
+
+// Two-exponential model f4a by variable projection (Golub & Pereyra, SIAM J.
+// Numer. Anal. 10, 1973): for rates p = (lam1, lam2) the amplitudes minimising
+// the weighted residual are linear least squares, so the cost is
+// 0.5 ||P_perp(p) w y||^2 with P_perp the projector onto the complement of
+// span{w e1, w e2}, e_i = exp(-(lam_i + lp) t).  Its Jacobian is Kaufman's
+// (BIT 15, 1975): column i = P_perp d(w e_i)/d lam_i c_i, exact at zero
+// residual.  The basis is orthonormalised by Gram-Schmidt with one
+// re-orthogonalisation, so nearly equal rates (cos(e1, e2) -> 1) keep a
+// residual accurate to rounding; numerically dependent columns (r22 below
+// 64 eps r11) give a non-finite cost, which the trust region rejects.
+// TM is a compile-time bound on the number of samples, so the per-sample
+// arrays stay in registers.  y is already multiplied by the weights.
+constexpr int M_F4A_VP8 = 10, M_F4A_VP16 = 11;
+template <int TM> struct VpTraits {
+  static constexpr int N = 2;
+  static constexpr bool VP = true;
+  static constexpr int TMAX = TM;
+};
+template <> struct ModelTraits<M_F4A_VP8> : VpTraits<8> {};
+template <> struct ModelTraits<M_F4A_VP16> : VpTraits<16> {};
+template <int M, typename = void> struct IsVp { static constexpr bool value = false; };
+template <int M> struct IsVp<M, decltype((void)ModelTraits<M>::VP)> { static constexpr bool value = ModelTraits<M>::VP; };
+
+template <int TM, typename R>
+struct VpBasis {
+  R e1[TM], e2[TM];  // weighted exponentials, then the orthonormal basis q1, q2
+  R r[TM];           // residual y - Phi c (weighted)
+  R r11, r12, r22, c1, c2;
+};
+
+template <int TM, typename R>
+__device__ __forceinline__ R vp_project(const FitArgs& a, const R* y, const R* p, VpBasis<TM, R>& b) {
+  const R lp = (R)a.lam_phys;
+  R n1 = (R)0;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    if (j < a.T) {
+      const R w = (R)a.w[j], t = (R)a.t[j];
+      b.e1[j] = w * exp(-(p[0] + lp) * t);
+      b.e2[j] = w * exp(-(p[1] + lp) * t);
+    } else {
+      b.e1[j] = (R)0;
+      b.e2[j] = (R)0;
+    }
+    n1 += b.e1[j] * b.e1[j];
+  }
+  b.r11 = sqrt(n1);
+  if (!(b.r11 > Lim<R>::tiny())) return (R)NAN;
+  R d = (R)0;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    b.e1[j] /= b.r11;
+    d += b.e1[j] * b.e2[j];
+  }
+  R d2 = (R)0;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    b.e2[j] -= d * b.e1[j];
+    d2 += b.e1[j] * b.e2[j];
+  }
+  R n2 = (R)0;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    b.e2[j] -= d2 * b.e1[j];
+    n2 += b.e2[j] * b.e2[j];
+  }
+  b.r12 = d + d2;
+  b.r22 = sqrt(n2);
+  if (!(b.r22 > (R)64 * Lim<R>::eps() * b.r11)) return (R)NAN;
+  R s1 = (R)0;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    b.e2[j] /= b.r22;
+    s1 += b.e1[j] * y[j];
+  }
+  R s2 = (R)0;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    b.r[j] = y[j] - s1 * b.e1[j];
+    s2 += b.e2[j] * b.r[j];
+  }
+  R cost = (R)0;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    b.r[j] -= s2 * b.e2[j];
+    cost += b.r[j] * b.r[j];
+  }
+  b.c2 = s2 / b.r22;
+  b.c1 = (s1 - b.r12 * b.c2) / b.r11;
+  return (R)0.5 * cost;
+}
+
+// normal equations of the projected problem; LM residual is Phi c - y = -r
+template <int TM, typename R>
+__device__ __forceinline__ R vp_normal_eq(const FitArgs& a, const R* y, const R* p, R* A, R* g) {
+  VpBasis<TM, R> b;
+  const R cost = vp_project<TM, R>(a, y, p, b);
+  if (!isfinite(cost)) {
+    A[0] = A[1] = A[2] = A[3] = g[0] = g[1] = (R)0;
+    return cost;
+  }
+  // d(w e_i)/d lam_i * c_i = -t w e_i c_i, rebuilt from q1, q2 and R: w e1 = r11 q1,
+  // w e2 = r12 q1 + r22 q2
+  R j1[TM], j2[TM];
+  R u1 = (R)0, u2 = (R)0, v1 = (R)0, v2 = (R)0;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    const R t = j < a.T ? (R)a.t[j] : (R)0;
+    const R we1 = b.r11 * b.e1[j], we2 = b.r12 * b.e1[j] + b.r22 * b.e2[j];
+    j1[j] = -t * we1 * b.c1;
+    j2[j] = -t * we2 * b.c2;
+    u1 += b.e1[j] * j1[j];
+    u2 += b.e1[j] * j2[j];
+  }
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    j1[j] -= u1 * b.e1[j];
+    j2[j] -= u2 * b.e1[j];
+    v1 += b.e2[j] * j1[j];
+    v2 += b.e2[j] * j2[j];
+  }
+  R a11 = (R)0, a12 = (R)0, a22 = (R)0, g1 = (R)0, g2 = (R)0;
+#pragma unroll
+  for (int j = 0; j < TM; ++j) {
+    j1[j] -= v1 * b.e2[j];
+    j2[j] -= v2 * b.e2[j];
+    a11 += j1[j] * j1[j];
+    a12 += j1[j] * j2[j];
+    a22 += j2[j] * j2[j];
+    g1 -= j1[j] * b.r[j];
+    g2 -= j2[j] * b.r[j];
+  }
+  A[0] = a11;
+  A[1] = a12;
+  A[2] = a12;
+  A[3] = a22;
+  g[0] = g1;
+  g[1] = g2;
+  return cost;
+}
+
 // normal equations at p: A = J^T J (upper triangle), g = J^T r, returns 0.5 r^T r
 template <int M, typename R>
 __device__ R normal_eq(const FitArgs& a, const R* y, const R* p, R* A, R* g) {
+  if constexpr (IsVp<M>::value) {
+    return vp_normal_eq<ModelTraits<M>::TMAX, R>(a, y, p, A, g);
+  } else {
   constexpr int N = ModelTraits<M>::N;
 #pragma unroll
   for (int i = 0; i < N * N; ++i) A[i] = (R)0;
@@ -213,10 +377,15 @@ __device__ R normal_eq(const FitArgs& a, const R* y, const R* p, R* A, R* g) {
     cost += r * r;
   }
   return (R)0.5 * cost;
+  }
 }
 
 template <int M, typename R>
 __device__ R cost_at(const FitArgs& a, const R* y, const R* p) {
+  if constexpr (IsVp<M>::value) {
+    VpBasis<ModelTraits<M>::TMAX, R> b;
+    return vp_project<ModelTraits<M>::TMAX, R>(a, y, p, b);
+  } else {
   constexpr int N = ModelTraits<M>::N;
   R cost = (R)0;
   for (int k = 0; k < a.T; ++k) {
@@ -225,21 +394,8 @@ __device__ R cost_at(const FitArgs& a, const R* y, const R* p) {
     cost += r * r;
   }
   return (R)0.5 * cost;
+  }
 }
-
-// tolerances per precision: MINPACK's defaults (sqrt(eps) ftol/xtol) in double; the
-// float iterations stop at 1e-6 and are followed by a double polish
-template <typename R> struct Lim;
-template <> struct Lim<double> {
-  static __device__ double tiny() { return 2.2250738585072014e-308; }
-  static __device__ double tol() { return 1.49012e-8; }
-  static __device__ double eps() { return 2.220446049250313e-16; }
-};
-template <> struct Lim<float> {
-  static __device__ float tiny() { return 1.17549435e-38f; }
-  static __device__ float tol() { return 1e-6f; }
-  static __device__ float eps() { return 1.1920929e-7f; }
-};
 
 // Cholesky of (A + par diag(D^2)) (A symmetric, upper triangle stored in A[i*N+c], c >= i).
 // L is lower triangular, row major.  false if not positive definite.
@@ -305,7 +461,8 @@ __device__ void lm_par(const R* A, const R* g, const R* D, R delta, R& par, R* p
   R L[N * N], w[N], q[N];
   R parl = (R)0.0;
   R fp;
-  if (chol_damped<N, R>(A, D, (R)0.0, L)) {
+  const bool have_gn = chol_damped<N, R>(A, D, (R)0.0, L);  // false: J^T J singular, no Gauss-Newton step
+  if (have_gn) {
     chol_solve_neg<N, R>(L, g, p);
     const R dxn = dnorm<N, R>(D, p);
     fp = dxn - delta;
@@ -329,7 +486,7 @@ __device__ void lm_par(const R* A, const R* g, const R* D, R delta, R& par, R* p
   if (paru == (R)0.0) paru = dwarf / fmin(delta, (R)0.1);
   par = fmax(par, parl);
   par = fmin(par, paru);
-  if (par == (R)0.0) par = gn / fmax(dnorm<N, R>(D, p), dwarf);
+  if (par == (R)0.0 && have_gn) par = gn / fmax(dnorm<N, R>(D, p), dwarf);  // else 0.001 paru below
   fp = (R)0.0;
   for (int it = 1; it <= 10; ++it) {
     if (par == (R)0.0) par = fmax(dwarf, (R)0.001 * paru);
@@ -443,33 +600,80 @@ __device__ int lm_fit(const FitArgs& a, const R* y, R* x, int maxfev) {
   }
 }
 
-// FP64 Gauss-Newton refinement of an FP32 least-squares solution: a few
-// normal-equation steps, each kept only if it lowers the FP64 cost.  False if
-// the cost is not finite.
+// Fallbacks of a failed fit, the AUC and the stores of one voxel.  good: the
+// minimiser converged (curve_fit raises for any other outcome).
 template <int M>
-__device__ bool polish_fp64(const FitArgs& a, const double* y, double* p) {
+__device__ __forceinline__ void store_fit(const FitArgs& a, double* p, bool good, double ymax, long long v, long long nvox,
+                                          double* __restrict__ params, double* __restrict__ auc,
+                                          unsigned char* __restrict__ ok, float* __restrict__ auc32) {
   constexpr int N = ModelTraits<M>::N;
-  double A[N * N], g[N], L[N * N], h[N], pn[N], D[N];
-  for (int it = 0; it < 4; ++it) {
-    const double F = normal_eq<M, double>(a, y, p, A, g);
-    if (!isfinite(F)) return false;
-    if (F == 0.0) return true;
-    double dmax = 0.0;
+  if (!good) {
+    if (M == M_MONO_LAMBDA) {  // fallback [0, lam_phys] (curve_fitting.py:58-59)
+      p[0] = 0.0;
+      p[1] = a.lam_phys;
+    } else {                   // fallback zeros (curve_fitting.py:210-213)
 #pragma unroll
-    for (int i = 0; i < N; ++i) dmax = fmax(dmax, A[i * N + i]);
-#pragma unroll
-    for (int i = 0; i < N; ++i) D[i] = 1.0;
-    if (!chol_damped<N, double>(A, D, 1e-14 * dmax, L)) return true;
-    chol_solve_neg<N, double>(L, g, h);
-#pragma unroll
-    for (int i = 0; i < N; ++i) pn[i] = p[i] + h[i];
-    const double Fn = cost_at<M, double>(a, y, pn);
-    if (!(Fn < F)) return true;
-#pragma unroll
-    for (int i = 0; i < N; ++i) p[i] = pn[i];
-    if (F - Fn <= 1e-15 * F) return true;
+      for (int i = 0; i < N; ++i) p[i] = 0.0;
+    }
   }
-  return true;
+#pragma unroll
+  for (int i = 0; i < N; ++i) params[(long long)i * nvox + v] = p[i];
+  double s = 0.0;
+  bool inf_done = false;
+  if (a.auc_inf && good) {  // integral of the fitted curve from 0 to infinity
+    if constexpr (M == M_MONO_LAMBDA) {
+      if (p[1] > 0.0) {
+        s = p[0] / p[1];
+        inf_done = true;
+      }
+    } else if constexpr (M == M_F2) {
+      const double k = p[1] + a.lam_phys;
+      if (k > 0.0) {
+        s = p[0] / k;
+        inf_done = true;
+      }
+    } else if constexpr (M == M_F4A) {
+      // A1 e^{-k1 t} + A2 e^{-k2 t} is >= 0 on [0, inf) iff the slow amplitude is
+      // >= 0 and A1 + A2 >= 0.  The part before the first sample is an
+      // extrapolation: a component that decays by orders of magnitude before
+      // it (a runaway fast rate whose amplitude no sample constrains) would
+      // dominate the integral, so the curve at t = 0 may not exceed 100 times
+      // the largest sample.  Otherwise there is no meaningful cumulated activity.
+      const double k1 = p[1] + a.lam_phys, k2 = p[3] + a.lam_phys;
+      const double a_slow = (k1 < k2) ? p[0] : p[2];
+      const double f0 = p[0] + p[2];
+      const bool nonneg = a_slow >= 0.0 && f0 >= -1e-9 * (fabs(p[0]) + fabs(p[2]));
+      if (k1 > 0.0 && k2 > 0.0 && nonneg && f0 <= 100.0 * ymax) {
+        s = p[0] / k1 + p[2] / k2;
+        inf_done = true;
+      }
+    }
+    if (inf_done && !(isfinite(s) && isfinite((float)(s * a.f32_scale)))) inf_done = false;
+    if (!inf_done) good = false;  // diverging or unsupported: the sampled-interval rule below
+  }
+  if (inf_done) {
+  } else if (M == M_MONO_LAMBDA) {
+    // A0 / lam * (1 - exp(-lam * limit))  (curve_fitting.py:74-84)
+    s = p[0] / p[1] * (1.0 - exp(-p[1] * a.auc_limit));
+  } else {
+    // trapezoid of the fitted curve over the sampled times (curve_fitting.py:215)
+    double j[N];
+    s = 0.0;
+    double fprev = ModelTraits<M>::template eval<double>(p, a.t[0], a.lam_phys, j);
+    for (int k = 1; k < a.T; ++k) {
+      const double f = ModelTraits<M>::template eval<double>(p, a.t[k], a.lam_phys, j);
+      s += 0.5 * (f + fprev) * (a.t[k] - a.t[k - 1]);
+      fprev = f;
+    }
+  }
+  float s32 = (float)(s * a.f32_scale);
+  if (!isfinite(s32)) {  // the float copy feeds a convolution: one inf would reach every voxel
+    s32 = 0.0f;
+    good = false;
+  }
+  auc[v] = s;
+  if (auc32) auc32[v] = s32;
+  if (ok) ok[v] = good ? 1 : 0;
 }
 
 template <int M>
@@ -506,66 +710,90 @@ __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long n
       for (int k = 0; k < a.T; ++k) yf[k] = (float)y[k];
 #pragma unroll
       for (int i = 0; i < N; ++i) pf[i] = (float)p[i];
-      info = lm_fit<M, float>(a, yf, pf, a.max_fev);
+      lm_fit<M, float>(a, yf, pf, a.max_fev);
+      bool pf_finite = true;
 #pragma unroll
-      for (int i = 0; i < N; ++i) p[i] = (double)pf[i];
-      if (info != 5 && info != -1) info = polish_fp64<M>(a, y, p) ? 1 : 5;
+      for (int i = 0; i < N; ++i) pf_finite = pf_finite && isfinite(pf[i]);
+      if (pf_finite) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) p[i] = (double)pf[i];
+      }
+      info = lm_fit<M, double>(a, y, p, a.max_fev);  // FP64 from the FP32 end point decides
     } else {
       info = lm_fit<M, double>(a, y, p, a.max_fev);
     }
-    bool good = info >= 1 && info <= 4;  // curve_fit raises for any other outcome
-    if (!good) {
-      if (M == M_MONO_LAMBDA) {  // fallback [0, lam_phys] (curve_fitting.py:58-59)
-        p[0] = 0.0;
-        p[1] = a.lam_phys;
-      } else {                   // fallback zeros (curve_fitting.py:210-213)
+    double ymax = 0.0;
+    for (int k = 0; k < a.T; ++k) ymax = fmax(ymax, fabs(y[k]));
+    store_fit<M>(a, p, info >= 1 && info <= 4, ymax, v, nvox, params, auc, ok, auc32);
+  }
+}
+
+
+// Variable-projection fit of f4a (PVD_FIT_VARPRO): LM over the two rates, then
+// the amplitudes at the converged rates in FP64; fast component stored first.
+template <int MV>
+__global__ void k_tac_fit_vp(FitArgs a, const float* __restrict__ acts, long long nvox, double* __restrict__ params,
+                             double* __restrict__ auc, unsigned char* __restrict__ ok, float* __restrict__ auc32) {
+  constexpr int TM = ModelTraits<MV>::TMAX;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvox; v += (long long)gridDim.x * blockDim.x) {
+    double y[TM];
+    bool finite = true;
 #pragma unroll
-        for (int i = 0; i < N; ++i) p[i] = 0.0;
-      }
+    for (int k = 0; k < TM; ++k) {
+      y[k] = k < a.T ? (double)__ldg(acts + (long long)k * nvox + v) : 0.0;
+      finite = finite && isfinite(y[k]);
     }
+    if (a.force_zero_at_t0) {
+      const double y0 = y[0];
 #pragma unroll
-    for (int i = 0; i < N; ++i) params[(long long)i * nvox + v] = p[i];
-    double s = 0.0;
-    bool inf_done = false;
-    if (a.auc_inf && good) {  // integral of the fitted curve from 0 to infinity
-      if constexpr (M == M_MONO_LAMBDA) {
-        if (p[1] > 0.0) {
-          s = p[0] / p[1];
-          inf_done = true;
-        }
-      } else if constexpr (M == M_F2) {
-        const double k = p[1] + a.lam_phys;
-        if (k > 0.0) {
-          s = p[0] / k;
-          inf_done = true;
-        }
-      } else if constexpr (M == M_F4A) {
-        const double k1 = p[1] + a.lam_phys, k2 = p[3] + a.lam_phys;
-        if (k1 > 0.0 && k2 > 0.0) {
-          s = p[0] / k1 + p[2] / k2;
-          inf_done = true;
+      for (int k = 1; k < TM; ++k)
+        if (k < a.T) y[k] -= y0;
+      y[0] = 0.0;
+    }
+    double p[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) p[i] = a.p0[i];
+    if (a.p0_peel && finite) {
+      double yA = 0.0, yB = 0.0;
+#pragma unroll
+      for (int k = 0; k < TM; ++k) {
+        if (k == a.T - 2) yA = y[k];
+        if (k == a.T - 1) yB = y[k];
+      }
+      peel_biexp4(a, y[0], y[1], yA, yB, a.t[a.T - 2], a.t[a.T - 1], p);
+    }
+    double yw[TM];
+#pragma unroll
+    for (int k = 0; k < TM; ++k) yw[k] = k < a.T ? a.w[k] * y[k] : 0.0;
+    double lam[2] = {p[1], p[3]};
+    int info = -1;
+    if (finite && a.T >= 4) {
+      if (a.mixed) {
+        float ywf[TM], lf[2] = {(float)lam[0], (float)lam[1]};
+#pragma unroll
+        for (int k = 0; k < TM; ++k) ywf[k] = (float)yw[k];
+        lm_fit<MV, float>(a, ywf, lf, a.max_fev);
+        if (isfinite(lf[0]) && isfinite(lf[1])) {
+          lam[0] = lf[0];
+          lam[1] = lf[1];
         }
       }
-      if (!inf_done) good = false;  // diverging or unsupported: the sampled-interval rule below
+      info = lm_fit<MV, double>(a, yw, lam, a.max_fev);
     }
-    if (inf_done) {
-    } else if (M == M_MONO_LAMBDA) {
-      // A0 / lam * (1 - exp(-lam * limit))  (curve_fitting.py:74-84)
-      s = p[0] / p[1] * (1.0 - exp(-p[1] * a.auc_limit));
-    } else {
-      // trapezoid of the fitted curve over the sampled times (curve_fitting.py:215)
-      double j[N];
-      s = 0.0;
-      double fprev = ModelTraits<M>::template eval<double>(p, a.t[0], a.lam_phys, j);
-      for (int k = 1; k < a.T; ++k) {
-        const double f = ModelTraits<M>::template eval<double>(p, a.t[k], a.lam_phys, j);
-        s += 0.5 * (f + fprev) * (a.t[k] - a.t[k - 1]);
-        fprev = f;
-      }
+    bool good = info >= 1 && info <= 4;
+    if (good) {
+      VpBasis<TM, double> b;
+      good = isfinite(vp_project<TM, double>(a, yw, lam, b));
+      const bool swap = lam[1] > lam[0];
+      p[0] = swap ? b.c2 : b.c1;
+      p[1] = swap ? lam[1] : lam[0];
+      p[2] = swap ? b.c1 : b.c2;
+      p[3] = swap ? lam[0] : lam[1];
     }
-    auc[v] = s;
-    if (auc32) auc32[v] = (float)(s * a.f32_scale);
-    if (ok) ok[v] = good ? 1 : 0;
+    double ymax = 0.0;
+#pragma unroll
+    for (int k = 0; k < TM; ++k) ymax = fmax(ymax, fabs(y[k]));
+    store_fit<M_F4A>(a, p, good, ymax, v, nvox, params, auc, ok, auc32);
   }
 }
 
@@ -604,9 +832,19 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
     return set_error(PVD_ERR_ARG, "pvd_tac_fit: PVD_FIT_P0_FROM_DATA applies to PVD_FIT_F4A");
   if ((flags & PVD_FIT_AUC_INF) && model != M_MONO_LAMBDA && model != M_F2 && model != M_F4A)
     return set_error(PVD_ERR_ARG, "pvd_tac_fit: PVD_FIT_AUC_INF applies to the mono, f2 and f4a models");
+  if ((flags & PVD_FIT_VARPRO) && model != M_F4A)
+    return set_error(PVD_ERR_ARG, "pvd_tac_fit: PVD_FIT_VARPRO applies to PVD_FIT_F4A");
   cudaStream_t st = (cudaStream_t)stream;
   const int threads = 128;
   const int blocks = (int)std::min<long long>((n_vox + threads - 1) / threads, 152LL * 64);
+  if (flags & PVD_FIT_VARPRO) {
+    if (n_times <= 8)
+      k_tac_fit_vp<M_F4A_VP8><<<blocks, threads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
+    else
+      k_tac_fit_vp<M_F4A_VP16><<<blocks, threads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
+    PVD_LAUNCH_CHECK("k_tac_fit_vp");
+    return PVD_OK;
+  }
   switch (model) {
 #define PVD_FIT_CASE(M)                                                                    \
   case M:                                                                                  \

@@ -36,6 +36,25 @@ def test_errors_without_gpu_are_status_codes():
     assert lib.pvd_conv_execute(None, None, None, None, ctypes.c_float(1.0), None) == 1
 
 
+def test_fit_flag_validation_happens_before_any_cuda_call():
+    lib = _native.load()
+    t = (ctypes.c_double * 4)(1.0, 4.0, 24.0, 96.0)
+    p0 = (ctypes.c_double * 5)(1.0, 0.1, 0.5, 0.01, 0.0)
+    fake = ctypes.c_void_p(16)  # never dereferenced: every call below fails validation first
+
+    def fit(model, flags, n_times=4, max_fev=100):
+        return lib.pvd_tac_fit(model, t, None, n_times, p0, 0.0, 0.0, max_fev, flags, fake, 10,
+                               fake, fake, None, None, 1.0, None)
+
+    assert fit(_native.PVD_FIT_F2, _native.PVD_FIT_VARPRO) == 1
+    assert "PVD_FIT_VARPRO" in _native.last_error()
+    assert fit(_native.PVD_FIT_F3, _native.PVD_FIT_AUC_INF) == 1
+    assert fit(_native.PVD_FIT_F2, _native.PVD_FIT_P0_FROM_DATA) == 1
+    assert fit(_native.PVD_FIT_F4A, _native.PVD_FIT_VARPRO, n_times=17) == 1
+    assert fit(_native.PVD_FIT_F4A, _native.PVD_FIT_VARPRO, max_fev=0) == 1
+    assert fit(42, 0) == 1
+
+
 def test_fast_length_registry():
     from tests.test_conv_gpu import FAST_LENGTHS
     lens = _native.fast_lengths()
