@@ -233,8 +233,8 @@ enum {
  * positive, the f4a curve non-negative on [0, inf) and at t = 0 at most 100
  * times the largest sample, and the integral finite;
  * otherwise the voxel is marked not ok and the model's own AUC rule is used).  PVD_FIT_MIXED runs the iterations in FP32, then the same minimiser
- * again in FP64 from where they stopped; success is decided by the FP64 run's
- * convergence tests alone.  PVD_FIT_VARPRO (f4a only) minimises the same
+ * again in FP64 from where they stopped, with at most 60 evaluations; success
+ * is decided by the FP64 run's convergence tests alone.  PVD_FIT_VARPRO (f4a only) minimises the same
  * least-squares cost by variable projection: the two amplitudes are solved
  * linearly for given rates and the trust-region iteration runs over the two
  * rates only, which converges where the four-parameter iteration stalls in the
@@ -317,6 +317,53 @@ pvd_status pvd_mc_run(pvd_mc_plan* plan, const float* activity_d, const float* d
                       pvd_stream stream);
 
 pvd_status pvd_mc_plan_destroy(pvd_mc_plan* plan);
+
+/* ------------------------------------------------------------------------ */
+/* Batched time-integrated dose                                               */
+/* ------------------------------------------------------------------------ */
+
+/* One volume of a batch: n_times activity maps at their times, fitted per
+ * voxel with the two-exponential model f4a from an exponential-peeling start
+ * (pvd_tac_fit with PVD_FIT_P0_FROM_DATA | PVD_FIT_AUC_INF and the caller's
+ * flags), the fit's integral from 0 to infinity times time_scale (e.g. 3600
+ * for hours -> seconds) as float32 cumulated activity in cum_d, and that
+ * convolved with every kernel slot of the plan into dose_d (pvd_conv_execute,
+ * density-scaled when density_d is given).  The reference computes this one
+ * volume at a time on the CPU: core/dose_calculator.py:85-164 with
+ * time_integration/curve_fitting.py:112-219 and core/kernel_convolution.py:48-106. */
+typedef struct {
+  pvd_plan* plan;               /* plan of this volume's shape; items may share a plan */
+  const float* activity_d;      /* device float32 [n_times][n_vox] */
+  const double* times;          /* host, n_times entries (read during the call) */
+  int n_times;                  /* 4 .. PVD_MAX_TIMEPOINTS */
+  const float* density_d;       /* device float32 [n_vox] or NULL */
+  double* params_d;             /* device float64 [4][n_vox] */
+  double* auc_d;                /* device float64 [n_vox] */
+  unsigned char* ok_d;          /* device uint8 [n_vox] or NULL */
+  float* cum_d;                 /* device float32 [n_vox] */
+  float* dose_d;                /* device float32 [n_kernels][n_vox] */
+} pvd_batch_item;
+
+/* Enqueue every item on `stream`, item by item (fit, then convolution).
+ * fit_flags: further PVD_FIT_* flags (PVD_FIT_VARPRO, PVD_FIT_MIXED);
+ * max_fev: the fit's evaluation budget per voxel.  All items are validated
+ * before anything is enqueued.  May be recorded into a CUDA graph. */
+pvd_status pvd_batch_execute(const pvd_batch_item* items, int n_items, int fit_flags, int max_fev,
+                             double time_scale, pvd_stream stream);
+
+typedef struct pvd_batch pvd_batch;
+
+/* Run pvd_batch_execute of these items once on a private stream (loading every
+ * kernel it uses), then record it into a CUDA graph owned by the returned
+ * handle.  The items' buffers and plans must outlive the handle; their
+ * contents may change between runs. */
+pvd_status pvd_batch_create(const pvd_batch_item* items, int n_items, int fit_flags, int max_fev,
+                            double time_scale, pvd_batch** out);
+
+/* Launch the recorded graph on `stream`: the whole batch in one launch. */
+pvd_status pvd_batch_run(pvd_batch* batch, pvd_stream stream);
+
+pvd_status pvd_batch_destroy(pvd_batch* batch);
 
 /* ------------------------------------------------------------------------ */
 /* Misc                                                                       */

@@ -40,6 +40,7 @@ EXPORTED_SYMBOLS = [
     "pvd_fast_lengths", "pvd_plan_profile", "pvd_plan_pass_times",
     "pvd_weighted_sum", "pvd_tac_fit",
     "pvd_mc_plan_create", "pvd_mc_run", "pvd_mc_plan_destroy",
+    "pvd_batch_execute", "pvd_batch_create", "pvd_batch_run", "pvd_batch_destroy",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
 ]
 
@@ -69,6 +70,12 @@ class McDesc(C.Structure):
 class McStats(C.Structure):
     _fields_ = [("total_weight", C.c_ulonglong), ("emitted", C.c_ulonglong), ("escaped", C.c_ulonglong),
                 ("steps", C.c_ulonglong), ("activity_bq", C.c_double)]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("plan", C.c_void_p), ("activity_d", C.c_void_p), ("times", C.c_void_p), ("n_times", C.c_int),
+                ("density_d", C.c_void_p), ("params_d", C.c_void_p), ("auc_d", C.c_void_p), ("ok_d", C.c_void_p),
+                ("cum_d", C.c_void_p), ("dose_d", C.c_void_p)]
 
 
 class PlanInfo(C.Structure):
@@ -121,6 +128,10 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_mc_plan_create": (st, [C.POINTER(McDesc), C.POINTER(vp)]),
         "pvd_mc_run": (st, [vp, vp, vp, C.c_ulonglong, C.c_ulonglong, vp, vp, C.POINTER(McStats), vp]),
         "pvd_mc_plan_destroy": (st, [vp]),
+        "pvd_batch_execute": (st, [C.POINTER(BatchItem), i, i, i, d, vp]),
+        "pvd_batch_create": (st, [C.POINTER(BatchItem), i, i, i, d, C.POINTER(vp)]),
+        "pvd_batch_run": (st, [vp, vp]),
+        "pvd_batch_destroy": (st, [vp]),
         "pvd_last_error": (st, [C.c_char_p, C.c_size_t]),
         "pvd_version": (i, []),
         "pvd_launch_count": (C.c_uint64, [i]),

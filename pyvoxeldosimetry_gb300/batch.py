@@ -8,9 +8,11 @@ convergence tests decide success), its analytic integral to infinity as
 cumulated activity, and the dose-point-kernel convolution of that
 cumulated activity (``pvd_conv_execute``; density-scaled when a density map is
 given), giving absorbed dose in Gy.  ``prepare`` builds one convolution plan per
-distinct (shape, voxel size), allocates every buffer, and captures all the
-volumes' kernel launches in a single CUDA graph; ``run`` replays it, so the
-whole batch is one launch from the host.
+distinct (shape, voxel size), allocates every buffer, and has the native batch
+runtime (``pvd_batch_create``) record all the volumes' kernel launches in one
+CUDA graph; ``run`` launches it (``pvd_batch_run``), so the whole batch is one
+launch from the host.  Without the graph, ``run`` enqueues the same work
+directly (``pvd_batch_execute``).
 
 This is the batched workload the dose calculator serves many patients,
 timepoints and grid sizes with; the reference processes one volume at a time
@@ -20,7 +22,7 @@ time_integration/curve_fitting.py:112-219).
 from __future__ import annotations
 
 import ctypes as C
-from typing import Dict, List, Optional, Sequence
+from typing import Dict, List, Sequence
 
 import numpy as np
 import torch
@@ -30,7 +32,6 @@ from .conv import ConvPlan, _require_cuda
 from .data import nuclides as nd
 
 SECONDS_PER_HOUR = 3600.0
-F4A = 4
 
 
 class BatchDoseCalculator:
@@ -47,7 +48,8 @@ class BatchDoseCalculator:
         self._lib = N.load()
         self._plans: Dict[tuple, ConvPlan] = {}
         self._items: List[dict] = []
-        self._graph: Optional[torch.cuda.CUDAGraph] = None
+        self._desc = None          # pvd_batch_item array
+        self._batch = None         # pvd_batch handle (recorded graph)
 
     # -- setup ------------------------------------------------------------------
     def _plan(self, shape, vs) -> ConvPlan:
@@ -69,8 +71,8 @@ class BatchDoseCalculator:
     def prepare(self, volumes: Sequence[dict]) -> None:
         """``volumes``: dicts with ``activity`` (CUDA float32 [T, n0, n1, n2]), ``times``
         (T hours), ``voxel_size`` (mm, 3) and optional ``density`` (CUDA float32)."""
+        self._release_batch()
         self._items = []
-        self._graph = None
         for v in volumes:
             act = v["activity"]
             if not (isinstance(act, torch.Tensor) and act.is_cuda and act.dtype == torch.float32 and act.dim() == 4):
@@ -95,29 +97,36 @@ class BatchDoseCalculator:
                 "dose": torch.empty((1, *shape), dtype=torch.float32, device=self.device),
             }
             self._items.append(item)
-        if self.use_graph:
-            side = torch.cuda.Stream(self.device)
-            side.wait_stream(torch.cuda.current_stream(self.device))
-            with torch.cuda.stream(side):
-                self._launch_all()  # one eager pass before capture
-            torch.cuda.current_stream(self.device).wait_stream(side)
-            torch.cuda.synchronize(self.device)
-            self._graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(self._graph):
-                self._launch_all()
+        desc = (N.BatchItem * len(self._items))()
+        for d, it in zip(desc, self._items):
+            it["times_c"] = (C.c_double * len(it["times"]))(*it["times"])
+            d.plan = it["plan"]._h
+            d.activity_d = it["act"].data_ptr()
+            d.times = C.cast(it["times_c"], C.c_void_p)
+            d.n_times = len(it["times"])
+            d.density_d = it["rho"].data_ptr() if it["rho"] is not None else None
+            d.params_d = it["params"].data_ptr()
+            d.auc_d = it["auc"].data_ptr()
+            d.ok_d = it["ok"].data_ptr()
+            d.cum_d = it["cum"].data_ptr()
+            d.dose_d = it["dose"].data_ptr()
+        self._desc = desc
+        if self.use_graph and self._items:
+            h = C.c_void_p()
+            with torch.cuda.device(self.device):
+                torch.cuda.current_stream(self.device).synchronize()  # inputs written on torch's stream
+                N.check(self._lib.pvd_batch_create(desc, len(self._items), self._fit_flags(), self.max_fev,
+                                                   SECONDS_PER_HOUR, C.byref(h)))
+            self._batch = h
 
-    def _launch_all(self) -> None:
-        flags = (N.PVD_FIT_P0_FROM_DATA | N.PVD_FIT_AUC_INF | N.PVD_FIT_VARPRO
-                 | (N.PVD_FIT_MIXED if self.mixed_fit else 0))
-        p0 = (C.c_double * 5)(1.0, 0.1, 0.5, 0.01, 0.0)
-        sh = torch.cuda.current_stream(self.device).cuda_stream
-        for it in self._items:
-            t = (C.c_double * len(it["times"]))(*it["times"])
-            N.check(self._lib.pvd_tac_fit(F4A, t, None, len(it["times"]), p0, 0.0, 0.0, self.max_fev, flags,
-                                          it["act"].data_ptr(), it["nvox"], it["params"].data_ptr(),
-                                          it["auc"].data_ptr(), it["ok"].data_ptr(), it["cum"].data_ptr(),
-                                          SECONDS_PER_HOUR, sh))
-            it["plan"].execute(it["cum"], density=it["rho"], out=it["dose"])
+    def _fit_flags(self) -> int:
+        return N.PVD_FIT_VARPRO | (N.PVD_FIT_MIXED if self.mixed_fit else 0)
+
+    def _release_batch(self) -> None:
+        if self._batch is not None:
+            self._lib.pvd_batch_destroy(self._batch)
+            self._batch = None
+        self._desc = None
 
     # -- execution --------------------------------------------------------------
     def run(self) -> List[torch.Tensor]:
@@ -125,10 +134,12 @@ class BatchDoseCalculator:
         if not self._items:
             return []
         with torch.cuda.device(self.device):
-            if self._graph is not None:
-                self._graph.replay()
+            sh = torch.cuda.current_stream(self.device).cuda_stream
+            if self._batch is not None:
+                N.check(self._lib.pvd_batch_run(self._batch, sh))
             else:
-                self._launch_all()
+                N.check(self._lib.pvd_batch_execute(self._desc, len(self._items), self._fit_flags(),
+                                                    self.max_fev, SECONDS_PER_HOUR, sh))
         return [it["dose"][0] for it in self._items]
 
     def calculate(self, volumes: Sequence[dict]) -> List[torch.Tensor]:
@@ -141,8 +152,14 @@ class BatchDoseCalculator:
         shape = tuple(it["cum"].shape)
         return it["params"].view(4, *shape), it["auc"].view(shape), it["ok"].view(shape).bool()
 
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
     def close(self) -> None:
-        self._graph = None
+        self._release_batch()
         self._items = []
         for p in self._plans.values():
             p.close()

@@ -220,12 +220,14 @@ template <> struct Lim<float> {
 // 64 eps r11) give a non-finite cost, which the trust region rejects.
 // TM is a compile-time bound on the number of samples, so the per-sample
 // arrays stay in registers.  y is already multiplied by the weights.
-constexpr int M_F4A_VP8 = 10, M_F4A_VP16 = 11;
+constexpr int M_F4A_VP4 = 10, M_F4A_VP6 = 11, M_F4A_VP8 = 12, M_F4A_VP16 = 13;
 template <int TM> struct VpTraits {
   static constexpr int N = 2;
   static constexpr bool VP = true;
   static constexpr int TMAX = TM;
 };
+template <> struct ModelTraits<M_F4A_VP4> : VpTraits<4> {};
+template <> struct ModelTraits<M_F4A_VP6> : VpTraits<6> {};
 template <> struct ModelTraits<M_F4A_VP8> : VpTraits<8> {};
 template <> struct ModelTraits<M_F4A_VP16> : VpTraits<16> {};
 template <int M, typename = void> struct IsVp { static constexpr bool value = false; };
@@ -516,15 +518,17 @@ __device__ void lm_par(const R* A, const R* g, const R* D, R delta, R& par, R* p
 // analytic Jacobian.  Returns MINPACK's info code: 1-4 success (ftol / xtol /
 // both / gtol), 5 evaluation budget exhausted, 6-8 tolerances too small, -1
 // non-finite cost.  `maxfev` counts model evaluations as a forward-difference
-// Jacobian would (N per Jacobian), so the budget matches curve_fit's.
+// Jacobian would (N per Jacobian), so the budget matches curve_fit's.  fstop > 0
+// adds a success test (info 1): residual norm <= fstop.
 template <int M, typename R>
-__device__ int lm_fit(const FitArgs& a, const R* y, R* x, int maxfev) {
+__device__ int lm_fit(const FitArgs& a, const R* y, R* x, int maxfev, R fstop = (R)0) {
   constexpr int N = ModelTraits<M>::N;
   const R ftol = Lim<R>::tol(), xtol = Lim<R>::tol(), epsmch = Lim<R>::eps();
   R A[N * N], g[N], D[N], p[N], xt[N];
   int nfev = 1;
   R fnorm = sqrt((R)2.0 * cost_at<M, R>(a, y, x));
   if (!isfinite(fnorm)) return -1;
+  if (fnorm <= fstop) return 1;
   R delta = (R)0.0, xnorm = (R)0.0, par = (R)0.0;
   for (int iter = 1;; ++iter) {
     normal_eq<M, R>(a, y, x, A, g);
@@ -587,6 +591,7 @@ __device__ int lm_fit(const FitArgs& a, const R* y, R* x, int maxfev) {
         for (int j = 0; j < N; ++j) x[j] = xt[j];
         fnorm = fnorm1;
         xnorm = dnorm<N, R>(D, x);
+        if (fnorm <= fstop) return 1;  // the curve reproduces the samples to their own precision
       }
       int info = 0;
       if (fabs(actred) <= ftol && prered <= ftol && (R)0.5 * ratio <= (R)1.0) info = 1;
@@ -676,6 +681,13 @@ __device__ __forceinline__ void store_fit(const FitArgs& a, double* p, bool good
   if (ok) ok[v] = good ? 1 : 0;
 }
 
+// Evaluation budget of the FP64 stage that finishes an FP32 fit: from an FP32
+// least-squares point the iteration converges quadratically in two or three
+// steps; 60 evaluations also cover slow cases, and a voxel that needs more
+// (FP64 runs at a small fraction of the FP32 rate, and one voxel holds its
+// whole warp) is reported as not converged.
+constexpr int kFinishFev = 60;
+
 template <int M>
 __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long nvox, double* __restrict__ params,
                           double* __restrict__ auc, unsigned char* __restrict__ ok, float* __restrict__ auc32) {
@@ -718,7 +730,7 @@ __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long n
 #pragma unroll
         for (int i = 0; i < N; ++i) p[i] = (double)pf[i];
       }
-      info = lm_fit<M, double>(a, y, p, a.max_fev);  // FP64 from the FP32 end point decides
+      info = lm_fit<M, double>(a, y, p, min(a.max_fev, kFinishFev));  // FP64 from the FP32 end point decides
     } else {
       info = lm_fit<M, double>(a, y, p, a.max_fev);
     }
@@ -729,71 +741,152 @@ __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long n
 }
 
 
-// Variable-projection fit of f4a (PVD_FIT_VARPRO): LM over the two rates, then
-// the amplitudes at the converged rates in FP64; fast component stored first.
+// Variable-projection fit of f4a (PVD_FIT_VARPRO), one thread per voxel with
+// load balancing inside each block.  Phase 1 (every voxel): exponential-peeling
+// start, the FP32 iteration (PVD_FIT_MIXED) and at most kShortFev FP64
+// evaluations.  Most voxels converge there.  The rest (nearly equal rates: the
+// projected cost has a long curved valley that the trust region crosses in
+// many small steps) go to a queue in shared memory with their current rates;
+// each time 128 are queued the whole block continues them in FP64 with the
+// full budget, so the long iterations run in full warps instead of holding a
+// warp of finished voxels each.  FP64 iterations also stop once the curve
+// reproduces the float32 samples to their rounding (2^-24 relative each).
+// The amplitudes are then solved at the converged rates in FP64; the fast
+// component is stored first.
+constexpr int kVpThreads = 128;
+constexpr int kShortFev = 30;  // FP64 evaluations in phase 1
+
+template <int TM>
+struct VpVoxel {
+  double y[TM], yw[TM];
+  double fstop;
+  bool finite;
+};
+
+template <int TM>
+__device__ __forceinline__ void vp_load(const FitArgs& a, const float* __restrict__ acts, long long nvox, long long v,
+                                        VpVoxel<TM>& d) {
+  d.finite = true;
+#pragma unroll
+  for (int k = 0; k < TM; ++k) {
+    d.y[k] = k < a.T ? (double)__ldg(acts + (long long)k * nvox + v) : 0.0;
+    d.finite = d.finite && isfinite(d.y[k]);
+  }
+  if (a.force_zero_at_t0) {
+    const double y0 = d.y[0];
+#pragma unroll
+    for (int k = 1; k < TM; ++k)
+      if (k < a.T) d.y[k] -= y0;
+    d.y[0] = 0.0;
+  }
+  double yn = 0.0;
+#pragma unroll
+  for (int k = 0; k < TM; ++k) {
+    d.yw[k] = k < a.T ? a.w[k] * d.y[k] : 0.0;
+    yn += d.yw[k] * d.yw[k];
+  }
+  // float32 samples carry relative rounding <= 2^-24 each: a fitted curve within
+  // twice that of the samples reproduces them to their own precision
+  d.fstop = 2.0 * 5.9604644775390625e-8 * sqrt(yn);
+}
+
+// amplitudes at the final rates, fallbacks, AUC and stores
+template <int TM>
+__device__ __forceinline__ void vp_store(const FitArgs& a, const VpVoxel<TM>& d, const double* lam, bool good,
+                                         long long v, long long nvox, double* __restrict__ params,
+                                         double* __restrict__ auc, unsigned char* __restrict__ ok,
+                                         float* __restrict__ auc32) {
+  double p[4] = {0.0, 0.0, 0.0, 0.0};
+  if (good) {
+    VpBasis<TM, double> b;
+    good = isfinite(vp_project<TM, double>(a, d.yw, lam, b));
+    const bool swap = lam[1] > lam[0];
+    p[0] = swap ? b.c2 : b.c1;
+    p[1] = swap ? lam[1] : lam[0];
+    p[2] = swap ? b.c1 : b.c2;
+    p[3] = swap ? lam[0] : lam[1];
+  }
+  double ymax = 0.0;
+#pragma unroll
+  for (int k = 0; k < TM; ++k) ymax = fmax(ymax, fabs(d.y[k]));
+  store_fit<M_F4A>(a, p, good, ymax, v, nvox, params, auc, ok, auc32);
+}
+
 template <int MV>
-__global__ void k_tac_fit_vp(FitArgs a, const float* __restrict__ acts, long long nvox, double* __restrict__ params,
-                             double* __restrict__ auc, unsigned char* __restrict__ ok, float* __restrict__ auc32) {
+__global__ void __launch_bounds__(kVpThreads) k_tac_fit_vp(FitArgs a, const float* __restrict__ acts, long long nvox,
+                                                           double* __restrict__ params, double* __restrict__ auc,
+                                                           unsigned char* __restrict__ ok, float* __restrict__ auc32) {
   constexpr int TM = ModelTraits<MV>::TMAX;
-  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvox; v += (long long)gridDim.x * blockDim.x) {
-    double y[TM];
-    bool finite = true;
+  __shared__ long long q_vox[2 * kVpThreads];
+  __shared__ double q_lam[2 * kVpThreads][2];
+  __shared__ int q_n;
+  const int tid = threadIdx.x;
+  if (tid == 0) q_n = 0;
+  __syncthreads();
+  for (long long base = (long long)blockIdx.x * kVpThreads; base < nvox; base += (long long)gridDim.x * kVpThreads) {
+    const long long v = base + tid;
+    if (v < nvox) {  // phase 1
+      VpVoxel<TM> d;
+      vp_load<TM>(a, acts, nvox, v, d);
+      double p[4];
 #pragma unroll
-    for (int k = 0; k < TM; ++k) {
-      y[k] = k < a.T ? (double)__ldg(acts + (long long)k * nvox + v) : 0.0;
-      finite = finite && isfinite(y[k]);
-    }
-    if (a.force_zero_at_t0) {
-      const double y0 = y[0];
+      for (int i = 0; i < 4; ++i) p[i] = a.p0[i];
+      if (a.p0_peel && d.finite) {
+        double yA = 0.0, yB = 0.0;
 #pragma unroll
-      for (int k = 1; k < TM; ++k)
-        if (k < a.T) y[k] -= y0;
-      y[0] = 0.0;
-    }
-    double p[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) p[i] = a.p0[i];
-    if (a.p0_peel && finite) {
-      double yA = 0.0, yB = 0.0;
-#pragma unroll
-      for (int k = 0; k < TM; ++k) {
-        if (k == a.T - 2) yA = y[k];
-        if (k == a.T - 1) yB = y[k];
-      }
-      peel_biexp4(a, y[0], y[1], yA, yB, a.t[a.T - 2], a.t[a.T - 1], p);
-    }
-    double yw[TM];
-#pragma unroll
-    for (int k = 0; k < TM; ++k) yw[k] = k < a.T ? a.w[k] * y[k] : 0.0;
-    double lam[2] = {p[1], p[3]};
-    int info = -1;
-    if (finite && a.T >= 4) {
-      if (a.mixed) {
-        float ywf[TM], lf[2] = {(float)lam[0], (float)lam[1]};
-#pragma unroll
-        for (int k = 0; k < TM; ++k) ywf[k] = (float)yw[k];
-        lm_fit<MV, float>(a, ywf, lf, a.max_fev);
-        if (isfinite(lf[0]) && isfinite(lf[1])) {
-          lam[0] = lf[0];
-          lam[1] = lf[1];
+        for (int k = 0; k < TM; ++k) {
+          if (k == a.T - 2) yA = d.y[k];
+          if (k == a.T - 1) yB = d.y[k];
         }
+        peel_biexp4(a, d.y[0], d.y[1], yA, yB, a.t[a.T - 2], a.t[a.T - 1], p);
       }
-      info = lm_fit<MV, double>(a, yw, lam, a.max_fev);
-    }
-    bool good = info >= 1 && info <= 4;
-    if (good) {
-      VpBasis<TM, double> b;
-      good = isfinite(vp_project<TM, double>(a, yw, lam, b));
-      const bool swap = lam[1] > lam[0];
-      p[0] = swap ? b.c2 : b.c1;
-      p[1] = swap ? lam[1] : lam[0];
-      p[2] = swap ? b.c1 : b.c2;
-      p[3] = swap ? lam[0] : lam[1];
-    }
-    double ymax = 0.0;
+      double lam[2] = {p[1], p[3]};
+      int info = -1;
+      if (d.finite && a.T >= 4) {
+        if (a.mixed) {
+          float ywf[TM], lf[2] = {(float)lam[0], (float)lam[1]};
 #pragma unroll
-    for (int k = 0; k < TM; ++k) ymax = fmax(ymax, fabs(y[k]));
-    store_fit<M_F4A>(a, p, good, ymax, v, nvox, params, auc, ok, auc32);
+          for (int k = 0; k < TM; ++k) ywf[k] = (float)d.yw[k];
+          lm_fit<MV, float>(a, ywf, lf, a.max_fev);
+          if (isfinite(lf[0]) && isfinite(lf[1])) {
+            lam[0] = lf[0];
+            lam[1] = lf[1];
+          }
+        }
+        info = lm_fit<MV, double>(a, d.yw, lam, min(a.max_fev, kShortFev), d.fstop);
+      }
+      if (info == 5 && a.max_fev > kShortFev && isfinite(lam[0]) && isfinite(lam[1])) {
+        const int pos = atomicAdd(&q_n, 1);  // < 2 * kVpThreads: drained below whenever it reaches kVpThreads
+        q_vox[pos] = v;
+        q_lam[pos][0] = lam[0];
+        q_lam[pos][1] = lam[1];
+      } else {
+        vp_store<TM>(a, d, lam, info >= 1 && info <= 4, v, nvox, params, auc, ok, auc32);
+      }
+    }
+    __syncthreads();
+    const int n = q_n;
+    if (n >= kVpThreads) {  // phase 2 on a full block of queued voxels
+      const int pos = n - kVpThreads + tid;
+      const long long vq = q_vox[pos];
+      double lam[2] = {q_lam[pos][0], q_lam[pos][1]};
+      __syncthreads();
+      if (tid == 0) q_n = n - kVpThreads;
+      VpVoxel<TM> d;
+      vp_load<TM>(a, acts, nvox, vq, d);
+      const int info = lm_fit<MV, double>(a, d.yw, lam, a.max_fev - kShortFev, d.fstop);
+      vp_store<TM>(a, d, lam, info >= 1 && info <= 4, vq, nvox, params, auc, ok, auc32);
+    }
+    __syncthreads();
+  }
+  const int n = q_n;  // the rest of the queue
+  if (tid < n) {
+    const long long vq = q_vox[tid];
+    double lam[2] = {q_lam[tid][0], q_lam[tid][1]};
+    VpVoxel<TM> d;
+    vp_load<TM>(a, acts, nvox, vq, d);
+    const int info = lm_fit<MV, double>(a, d.yw, lam, a.max_fev - kShortFev, d.fstop);
+    vp_store<TM>(a, d, lam, info >= 1 && info <= 4, vq, nvox, params, auc, ok, auc32);
   }
 }
 
@@ -838,10 +931,15 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
   const int threads = 128;
   const int blocks = (int)std::min<long long>((n_vox + threads - 1) / threads, 152LL * 64);
   if (flags & PVD_FIT_VARPRO) {
-    if (n_times <= 8)
-      k_tac_fit_vp<M_F4A_VP8><<<blocks, threads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
+    const int vblocks = (int)std::min<long long>((n_vox + kVpThreads - 1) / kVpThreads, 152LL * 16);
+    if (n_times == 4)
+      k_tac_fit_vp<M_F4A_VP4><<<vblocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
+    else if (n_times <= 6)
+      k_tac_fit_vp<M_F4A_VP6><<<vblocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
+    else if (n_times <= 8)
+      k_tac_fit_vp<M_F4A_VP8><<<vblocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
     else
-      k_tac_fit_vp<M_F4A_VP16><<<blocks, threads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
+      k_tac_fit_vp<M_F4A_VP16><<<vblocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
     PVD_LAUNCH_CHECK("k_tac_fit_vp");
     return PVD_OK;
   }

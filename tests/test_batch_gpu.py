@@ -56,7 +56,7 @@ def test_batch_dose_matches_truth_and_oracle(batch_case):
         rel = np.abs(fa - auc) / auc
         # 4 samples for 4 parameters: exact on noise-free data up to the float32 rounding of
         # the samples, which nearly equal half-lives and slow ones beyond the 96 h window amplify
-        assert np.median(rel[ok]) < 1e-6 and np.quantile(rel[ok], 0.99) < 1e-3 and rel[ok].max() < 1e-2
+        assert np.median(rel[ok]) < 1e-6 and np.quantile(rel[ok], 0.99) < 1e-3 and rel[ok].max() < 3e-2
         # convolution stage: the cumulated activity the fit produced (fallback rule where not ok)
         cum = fa.astype(np.float32).astype(np.float64) * 3600.0
         ref = oc.density_scale(oc.linear_conv_same(cum, kernel_S("Y90", vs)), rho)
@@ -122,10 +122,11 @@ def test_graph_replay_equals_eager_and_mixed_equals_fp64(batch_case):
         _, auc_d, ok_d = f64.fit_results(i)
         both = (ok_m & ok_d)
         rel = ((auc_m - auc_d).abs() / auc_d.abs())[both]
-        # both stop on the FP64 convergence tests (relative rate change 1.5e-8), from different starts
+        # both stop in FP64 once the curve reproduces the float32 samples to their rounding,
+        # from different starts: they agree to the precision the samples carry
         assert float(both.float().mean()) > 0.99
         assert float((ok_m ^ ok_d).float().mean()) < 3e-3
-        assert float(rel.median()) < 1e-7 and float(torch.quantile(rel.float(), 0.99)) < 1e-5
+        assert float(rel.median()) < 1e-6 and float(torch.quantile(rel.float(), 0.99)) < 2e-3
         assert torch.isfinite(df[i]).all()
     for c in (g, e, f64):
         c.close()

@@ -55,6 +55,29 @@ def test_fit_flag_validation_happens_before_any_cuda_call():
     assert fit(42, 0) == 1
 
 
+def test_batch_validation_happens_before_any_cuda_call():
+    lib = _native.load()
+    t = (ctypes.c_double * 4)(1.0, 4.0, 24.0, 96.0)
+    it = (_native.BatchItem * 1)()
+    for f in ("plan", "activity_d", "params_d", "auc_d", "cum_d", "dose_d"):
+        setattr(it[0], f, 16)  # never dereferenced: validation fails before the plan is looked at
+    it[0].times = ctypes.cast(t, ctypes.c_void_p)
+    it[0].n_times = 3
+    assert lib.pvd_batch_execute(it, 1, 0, 100, 3600.0, None) == 1
+    assert "n_times" in _native.last_error()
+    it[0].n_times = 4
+    t[2] = 4.0
+    assert lib.pvd_batch_execute(it, 1, 0, 100, 3600.0, None) == 1
+    assert "increase" in _native.last_error()
+    it[0].plan = None
+    assert lib.pvd_batch_execute(it, 1, 0, 100, 3600.0, None) == 1
+    assert lib.pvd_batch_execute(it, 1, 0, 0, 3600.0, None) == 1
+    h = ctypes.c_void_p()
+    assert lib.pvd_batch_create(it, 1, 0, 100, 3600.0, ctypes.byref(h)) == 1 and not h.value
+    assert lib.pvd_batch_run(None, None) == 1
+    assert lib.pvd_batch_destroy(None) == 0
+
+
 def test_fast_length_registry():
     from tests.test_conv_gpu import FAST_LENGTHS
     lens = _native.fast_lengths()
