@@ -52,7 +52,10 @@ WORKLOADS = {
                           ksize={"Y90": 15}, density=False),
 }
 PASS_NAMES = ["x_fwd", "y_fwd", "z_fwd_mul_inv", "y_inv", "x_inv"]
-PASS_KERNELS = ["k_x_fwd", "k_y<false>", "k_z", "k_y<true>", "k_x_inv"]
+PASS_KERNELS = ["kf_x_fwd", "kf_y<0>", "kf_z", "kf_y<1>", "kf_x_inv"]
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch, from one ncu --set full capture
+# of the same bench command (profiles/kf_x_inv_ct256_y90_lu177_i131.md)
+NCU_DRAM_BYTES_PER_LAUNCH = {"ct256_y90_lu177_i131": {"kf_x_inv": 142_640_128 + 37_710_592}}
 
 
 def make_inputs(wl):
@@ -268,6 +271,60 @@ def measure_fit(device, shape=(256, 256, 256), reps=2):
             "workload": "mono-exponential FP64 fit + AUC per voxel, 4 timepoints, 256^3"}
 
 
+def measure_vp_fit(device, shape=(256, 256, 256), reps=2):
+    """Per-voxel two-exponential fit by variable projection (FP32 iterations finished in
+    FP64) + analytic AUC, 4 timepoints of bi-exponential washout, half-lives 6..160 h."""
+    import ctypes as C
+    import torch
+    from pyvoxeldosimetry_gb300 import _native as N
+    lib = N.load()
+    times = [1.0, 4.0, 24.0, 96.0]
+    g = torch.Generator(device=device).manual_seed(3)
+    u = lambda: torch.rand(shape, generator=g, device=device)
+    a0 = u() ** 2 * 1e4 + 10.0
+    l1 = 0.6931471805599453 / (6.0 * (160.0 / 6.0) ** u())
+    l2 = 0.6931471805599453 / (6.0 * (160.0 / 6.0) ** u())
+    w = 0.2 + 0.6 * u()
+    acts = torch.stack([a0 * (w * torch.exp(-l1 * t) + (1 - w) * torch.exp(-l2 * t)) for t in times]).contiguous()
+    del a0, l1, l2, w
+    nv = int(np.prod(shape))
+    params = torch.empty((4, nv), dtype=torch.float64, device=device)
+    auc = torch.empty(nv, dtype=torch.float64, device=device)
+    ok = torch.empty(nv, dtype=torch.uint8, device=device)
+    t = (C.c_double * 4)(*times)
+    p0 = (C.c_double * 5)(1.0, 0.1, 0.5, 0.01, 0.0)
+    flags = N.PVD_FIT_P0_FROM_DATA | N.PVD_FIT_AUC_INF | N.PVD_FIT_VARPRO | N.PVD_FIT_MIXED
+    ms = []
+    for _ in range(reps + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        N.check(lib.pvd_tac_fit(N.PVD_FIT_F4A, t, None, 4, p0, 0.0, 0.0, 2000, flags, acts.data_ptr(), nv,
+                                params.data_ptr(), auc.data_ptr(), ok.data_ptr(), None, 1.0,
+                                torch.cuda.current_stream(device).cuda_stream))
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    tm = float(np.median(ms[1:]))
+    return {"value": nv / (tm / 1e3) / 1e9, "unit": "Gvoxel/s", "ms_per_run": tm, "voxels": nv,
+            "converged_fraction": float(ok.float().mean()),
+            "workload": f"two-exponential fit by variable projection (FP32 then FP64) + analytic AUC, "
+                        f"4 timepoints, {shape[0]}x{shape[1]}x{shape[2]}"}
+
+
+def run_only(args, device):
+    """One sub-measurement alone (a bounded case to profile), printed as its own JSON line."""
+    small = args.small
+    if args.only == "mc":
+        r = measure_mc(device, n_hist=1_000_000 if small else 10_000_000)
+    elif args.only == "fit":
+        r = measure_fit(device, shape=(128, 128, 128) if small else (256, 256, 256))
+    elif args.only == "vpfit":
+        r = measure_vp_fit(device, shape=(64, 128, 128) if small else (256, 256, 256))
+    else:
+        r = measure_batch(device, 2 if small else args.batch_volumes)
+    print(json.dumps({"only": args.only, "small": small, **r}), flush=True)
+
+
 def batch_volumes(device, n_volumes=64, seed=3, times=(1.0, 4.0, 24.0, 96.0), n_draw=64):
     """Uneven batch: n0, n1 ~ U{96..320}, n2 ~ U{96..256} (seeded), 4 timepoints of
     per-voxel bi-exponential washout A0 (w e^{-l1 t} + (1-w) e^{-l2 t}), half-lives
@@ -346,6 +403,9 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the MC, fit and batch sub-measurements")
     ap.add_argument("--batch-volumes", type=int, default=8,
                     help="volumes of the 64-volume seeded uneven batch to run in the batch sub-measurement")
+    ap.add_argument("--only", choices=["mc", "fit", "vpfit", "batch"],
+                    help="run one sub-measurement alone and print it (no contract line)")
+    ap.add_argument("--small", action="store_true", help="with --only: a bounded case for profiling")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     wl = WORKLOADS[args.workload]
@@ -364,6 +424,10 @@ def main():
     device = torch.device("cuda", local_rank)
     if world > 1:
         dist.init_process_group("nccl", device_id=device)
+
+    if args.only:
+        run_only(args, device)
+        return
 
     from pyvoxeldosimetry_gb300 import _native as N
     from pyvoxeldosimetry_gb300.core.kernel_convolution import KernelConvolutionCalculator
@@ -428,10 +492,7 @@ def main():
     dom = max(PASS_NAMES, key=lambda k: pass_ms[k])
     avg_s = pass_ms[dom] / max(pass_n[dom], 1) / 1e3
     achieved = bm[dom] / avg_s / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        traffic = json.loads(tf.read_text()).get(args.workload, {}).get(PASS_KERNELS[PASS_NAMES.index(dom)])
+    traffic = NCU_DRAM_BYTES_PER_LAUNCH.get(args.workload, {}).get(PASS_KERNELS[PASS_NAMES.index(dom)])
     step_s = total_ms / args.steps / 1e3
     roofline = {"bound": "hbm", "kernel": PASS_KERNELS[PASS_NAMES.index(dom)], "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
@@ -476,6 +537,7 @@ def main():
     if not args.no_extras:
         line["mc"] = measure_mc(device)
         line["tac_fit"] = measure_fit(device)
+        line["tac_fit_vp"] = measure_vp_fit(device)
         line["batch"] = measure_batch(device, args.batch_volumes)
 
     if rank == 0 and not args.no_cpu_baseline:
