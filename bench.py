@@ -311,6 +311,33 @@ def measure_vp_fit(device, shape=(256, 256, 256), reps=2):
                         f"4 timepoints, {shape[0]}x{shape[1]}x{shape[2]}"}
 
 
+def measure_dvh(device, shape=(256, 256, 256), bins=1000, reps=5):
+    """Dose-volume histogram (calculate_dvh): ROI statistics + histogram on the GPU,
+    edges and cumulative sum on the host; 10 algorithmic bytes per voxel (two passes
+    over a float32 dose and a uint8 mask)."""
+    import torch
+    from pyvoxeldosimetry_gb300.core.utils import calculate_dvh
+    g = torch.Generator(device=device).manual_seed(9)
+    dose = torch.rand(shape, generator=g, device=device) * 60.0
+    mask = (torch.rand(shape, generator=g, device=device) > 0.3).to(torch.uint8)
+    calculate_dvh(dose, mask, bins)
+    ms = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        calculate_dvh(dose, mask, bins)
+        e1.record()
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    t = float(np.median(ms))
+    nv = int(np.prod(shape))
+    peak, _ = load_peaks()
+    return {"value": nv / (t / 1e3) / 1e9, "unit": "Gvoxel/s", "ms_per_call": t, "voxels": nv, "bins": bins,
+            "hbm_frac": 10.0 * nv / (t / 1e3) / 1e9 / peak,
+            "workload": f"calculate_dvh, {shape[0]}x{shape[1]}x{shape[2]} float32 dose, uint8 ROI of 70 %, "
+                        "whole call (two device passes, two small host round trips)"}
+
+
 def run_only(args, device):
     """One sub-measurement alone (a bounded case to profile), printed as its own JSON line."""
     small = args.small
@@ -318,6 +345,8 @@ def run_only(args, device):
         r = measure_mc(device, n_hist=1_000_000 if small else 10_000_000)
     elif args.only == "fit":
         r = measure_fit(device, shape=(128, 128, 128) if small else (256, 256, 256))
+    elif args.only == "dvh":
+        r = measure_dvh(device, shape=(128, 128, 128) if small else (256, 256, 256))
     elif args.only == "vpfit":
         r = measure_vp_fit(device, shape=(64, 128, 128) if small else (256, 256, 256))
     else:
@@ -403,7 +432,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the MC, fit and batch sub-measurements")
     ap.add_argument("--batch-volumes", type=int, default=8,
                     help="volumes of the 64-volume seeded uneven batch to run in the batch sub-measurement")
-    ap.add_argument("--only", choices=["mc", "fit", "vpfit", "batch"],
+    ap.add_argument("--only", choices=["mc", "fit", "vpfit", "batch", "dvh"],
                     help="run one sub-measurement alone and print it (no contract line)")
     ap.add_argument("--small", action="store_true", help="with --only: a bounded case for profiling")
     args = ap.parse_args()
@@ -539,6 +568,7 @@ def main():
         line["tac_fit"] = measure_fit(device)
         line["tac_fit_vp"] = measure_vp_fit(device)
         line["batch"] = measure_batch(device, args.batch_volumes)
+        line["dvh"] = measure_dvh(device)
 
     if rank == 0 and not args.no_cpu_baseline:
         ks = reference_kernels(wl)

@@ -366,6 +366,37 @@ pvd_status pvd_batch_run(pvd_batch* batch, pvd_stream stream);
 pvd_status pvd_batch_destroy(pvd_batch* batch);
 
 /* ------------------------------------------------------------------------ */
+/* Dose-volume histogram                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces calculate_dvh (core/utils.py:233-262): np.histogram(dose[mask > 0],
+ * bins) with uniform bins between the ROI's minimum and maximum, then
+ * 1 - cumsum(hist) / n.  The device computes the ROI statistics and the
+ * counts; the caller computes the edges exactly as numpy does
+ * (np.linspace(first, last, bins + 1) in the dose's type, after widening an
+ * empty range by 0.5 on each side) and the cumulative sum.  The bin of every
+ * dose follows numpy's arithmetic for uniform bins operation for operation,
+ * so the counts equal np.histogram's.
+ * dose_d: device float32 or float64 [n]; mask_d: device uint8 or float32 [n]
+ * (voxels with mask > 0), or NULL for every voxel. */
+enum { PVD_DTYPE_U8 = 0, PVD_DTYPE_F32 = 1, PVD_DTYPE_F64 = 2 };
+typedef struct {
+  double min, max;       /* of the finite ROI doses (exact in the dose's type) */
+  long long count;       /* ROI voxels */
+  long long nonfinite;   /* ROI voxels whose dose is NaN or infinite */
+} pvd_roi_stats_t;
+
+/* ROI statistics; synchronises `stream` and fills *out. */
+pvd_status pvd_roi_stats(const void* dose_d, int dose_dtype, const void* mask_d, int mask_dtype, long long n,
+                         pvd_roi_stats_t* out, pvd_stream stream);
+
+/* counts_d[b] (device int64 [bins], overwritten) = ROI doses in bin b of the
+ * edges edges_d (device, dose type, bins + 1 values); doses outside
+ * [edges[0], edges[bins]] are not counted.  Enqueued on `stream`. */
+pvd_status pvd_histogram(const void* dose_d, int dose_dtype, const void* mask_d, int mask_dtype, long long n,
+                         const void* edges_d, int bins, long long* counts_d, pvd_stream stream);
+
+/* ------------------------------------------------------------------------ */
 /* Misc                                                                       */
 /* ------------------------------------------------------------------------ */
 

@@ -29,6 +29,7 @@ PVD_FIT_P0_FROM_DATA = 4
 PVD_FIT_AUC_INF = 8
 PVD_FIT_MIXED = 16
 PVD_FIT_VARPRO = 32
+PVD_DTYPE_U8, PVD_DTYPE_F32, PVD_DTYPE_F64 = 0, 1, 2
 PVD_MAX_KERNELS = 8
 PVD_MAX_TIMEPOINTS = 16
 
@@ -41,6 +42,7 @@ EXPORTED_SYMBOLS = [
     "pvd_weighted_sum", "pvd_tac_fit",
     "pvd_mc_plan_create", "pvd_mc_run", "pvd_mc_plan_destroy",
     "pvd_batch_execute", "pvd_batch_create", "pvd_batch_run", "pvd_batch_destroy",
+    "pvd_roi_stats", "pvd_histogram",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
 ]
 
@@ -76,6 +78,10 @@ class BatchItem(C.Structure):
     _fields_ = [("plan", C.c_void_p), ("activity_d", C.c_void_p), ("times", C.c_void_p), ("n_times", C.c_int),
                 ("density_d", C.c_void_p), ("params_d", C.c_void_p), ("auc_d", C.c_void_p), ("ok_d", C.c_void_p),
                 ("cum_d", C.c_void_p), ("dose_d", C.c_void_p)]
+
+
+class RoiStats(C.Structure):
+    _fields_ = [("min", C.c_double), ("max", C.c_double), ("count", C.c_longlong), ("nonfinite", C.c_longlong)]
 
 
 class PlanInfo(C.Structure):
@@ -132,6 +138,8 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_batch_create": (st, [C.POINTER(BatchItem), i, i, i, d, C.POINTER(vp)]),
         "pvd_batch_run": (st, [vp, vp]),
         "pvd_batch_destroy": (st, [vp]),
+        "pvd_roi_stats": (st, [vp, i, vp, i, C.c_longlong, C.POINTER(RoiStats), vp]),
+        "pvd_histogram": (st, [vp, i, vp, i, C.c_longlong, vp, i, vp, vp]),
         "pvd_last_error": (st, [C.c_char_p, C.c_size_t]),
         "pvd_version": (i, []),
         "pvd_launch_count": (C.c_uint64, [i]),

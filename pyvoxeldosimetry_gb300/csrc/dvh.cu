@@ -1,0 +1,227 @@
+// Dose-volume histogram on the GPU.
+//
+// Replaces calculate_dvh (pyvoxeldosimetry/core/utils.py:233-262): the doses
+// inside an ROI (mask > 0) are histogrammed with np.histogram(roi, bins) — bins
+// uniform between the ROI's minimum and maximum — and turned into 1 - cumsum / n.
+// Two HBM-bound passes over the volume:
+//   k_roi_stats  min, max, count and non-finite count of the ROI doses
+//                (numpy raises for a non-finite range; the host does too);
+//   k_histogram  the bin of every ROI dose by numpy's own arithmetic for
+//                uniform bins (numpy/lib/_histograms_impl.py, `histogram`):
+//                f = ((x - first) / (last - first)) * bins in the dose's type,
+//                truncated; index bins -> bins - 1; one step down if
+//                x < edge[i], one step up if x >= edge[i+1] and i != bins - 1,
+//                with the edges numpy's linspace produced (given by the host).
+//                Every operation is an IEEE round-to-nearest intrinsic, so the
+//                counts are the ones np.histogram returns, bit for bit.
+// Counts are accumulated per block in shared memory (bins <= kSmemBins), then
+// added to 64-bit global counters.
+#include <algorithm>
+#include <cstring>
+
+#include "pvd_common.cuh"
+
+namespace pvd {
+
+constexpr int kSmemBins = 12288;  // 48 KB of 32-bit counters
+constexpr int kDvhThreads = 256;
+
+__device__ __forceinline__ unsigned long long order_key(float x) {
+  const unsigned int b = __float_as_uint(x);
+  return (unsigned long long)((b & 0x80000000u) ? ~b : (b | 0x80000000u));
+}
+__device__ __forceinline__ unsigned long long order_key(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+template <typename M>
+__device__ __forceinline__ bool in_roi(const M* mask, long long i) {
+  return mask == nullptr || __ldg(mask + i) > (M)0;
+}
+
+// out[0] = min key, out[1] = max key, out[2] = ROI count, out[3] = non-finite ROI count
+template <typename T, typename M>
+__global__ void __launch_bounds__(kDvhThreads) k_roi_stats(const T* __restrict__ dose, const M* __restrict__ mask,
+                                                           long long n, unsigned long long* __restrict__ out) {
+  unsigned long long kmin = ~0ull, kmax = 0ull, cnt = 0ull, bad = 0ull;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+    if (!in_roi(mask, i)) continue;
+    const T x = __ldg(dose + i);
+    ++cnt;
+    if (!isfinite(x)) {
+      ++bad;
+      continue;
+    }
+    const unsigned long long k = order_key(x);
+    kmin = min(kmin, k);
+    kmax = max(kmax, k);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    kmin = min(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
+    kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, o));
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    bad += __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (cnt > bad) {
+      atomicMin(out + 0, kmin);
+      atomicMax(out + 1, kmax);
+    }
+    if (cnt) atomicAdd(out + 2, cnt);
+    if (bad) atomicAdd(out + 3, bad);
+  }
+}
+
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+template <typename T>
+__device__ __forceinline__ int bin_of(T x, T first, T denom, T nb, int bins, const T* __restrict__ edges) {
+  const T f = mul_rn(div_rn(sub_rn(x, first), denom), nb);
+  long long i = (long long)f;  // f >= 0: truncation, as astype(intp)
+  if (i >= bins) i = bins - 1;
+  if (i > 0 && x < __ldg(edges + i)) --i;
+  if (i != bins - 1 && x >= __ldg(edges + i + 1)) ++i;
+  return (int)i;
+}
+
+template <typename T, typename M, bool SMEM>
+__global__ void __launch_bounds__(kDvhThreads) k_histogram(const T* __restrict__ dose, const M* __restrict__ mask,
+                                                           long long n, const T* __restrict__ edges, int bins,
+                                                           unsigned long long* __restrict__ counts) {
+  __shared__ unsigned int h[SMEM ? kSmemBins : 1];
+  if (SMEM) {
+    for (int b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0u;
+    __syncthreads();
+  }
+  const T first = __ldg(edges), last = __ldg(edges + bins);
+  const T denom = sub_rn(last, first), nb = (T)bins;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+    if (!in_roi(mask, i)) continue;
+    const T x = __ldg(dose + i);
+    if (!(x >= first && x <= last)) continue;  // numpy keeps [first, last] only
+    const int b = bin_of<T>(x, first, denom, nb, bins, edges);
+    if (SMEM)
+      atomicAdd(h + b, 1u);
+    else
+      atomicAdd(counts + b, 1ull);
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int b = threadIdx.x; b < bins; b += blockDim.x)
+      if (h[b]) atomicAdd(counts + b, (unsigned long long)h[b]);
+  }
+}
+
+static int grid_for(long long n) {
+  return (int)std::max<long long>(1, std::min<long long>((n + kDvhThreads - 1) / kDvhThreads, 152LL * 8));
+}
+
+template <typename T, typename M>
+static void launch_stats(const void* dose, const void* mask, long long n, unsigned long long* out, cudaStream_t st) {
+  k_roi_stats<T, M><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n, out);
+}
+
+template <typename T, typename M>
+static void launch_hist(const void* dose, const void* mask, long long n, const void* edges, int bins,
+                        unsigned long long* counts, cudaStream_t st) {
+  if (bins <= kSmemBins)
+    k_histogram<T, M, true><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n,
+                                                                  (const T*)edges, bins, counts);
+  else
+    k_histogram<T, M, false><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n,
+                                                                   (const T*)edges, bins, counts);
+}
+
+static double key_to_value(unsigned long long k, int dtype) {
+  if (dtype == PVD_DTYPE_F32) {
+    const unsigned int u = (unsigned int)k;
+    const unsigned int b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+    float f;
+    std::memcpy(&f, &b, 4);
+    return (double)f;
+  }
+  const unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  double d;
+  std::memcpy(&d, &b, 8);
+  return d;
+}
+
+static bool dtypes_ok(int dose_dtype, int mask_dtype) {
+  return (dose_dtype == PVD_DTYPE_F32 || dose_dtype == PVD_DTYPE_F64) &&
+         (mask_dtype == PVD_DTYPE_U8 || mask_dtype == PVD_DTYPE_F32);
+}
+
+}  // namespace pvd
+
+using namespace pvd;
+
+extern "C" pvd_status pvd_roi_stats(const void* dose_d, int dose_dtype, const void* mask_d, int mask_dtype, long long n,
+                                    pvd_roi_stats_t* out, pvd_stream stream) {
+  if (!dose_d || !out) return set_error(PVD_ERR_ARG, "pvd_roi_stats: null argument");
+  if (n < 0) return set_error(PVD_ERR_ARG, "pvd_roi_stats: negative voxel count");
+  if (!dtypes_ok(dose_dtype, mask_dtype))
+    return set_error(PVD_ERR_ARG, "pvd_roi_stats: dose must be PVD_DTYPE_F32/F64, mask PVD_DTYPE_U8/F32");
+  out->min = 0.0;
+  out->max = 0.0;
+  out->count = 0;
+  out->nonfinite = 0;
+  if (n == 0) return PVD_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long* acc = nullptr;
+  cudaError_t e = cudaMallocAsync((void**)&acc, 4 * sizeof(unsigned long long), st);
+  if (e != cudaSuccess) return set_error(PVD_ERR_OOM, std::string("pvd_roi_stats: ") + cudaGetErrorString(e));
+  const unsigned long long init[4] = {~0ull, 0ull, 0ull, 0ull};
+  unsigned long long host[4];
+  e = cudaMemcpyAsync(acc, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    if (dose_dtype == PVD_DTYPE_F32)
+      (mask_dtype == PVD_DTYPE_U8) ? launch_stats<float, unsigned char>(dose_d, mask_d, n, acc, st)
+                                   : launch_stats<float, float>(dose_d, mask_d, n, acc, st);
+    else
+      (mask_dtype == PVD_DTYPE_U8) ? launch_stats<double, unsigned char>(dose_d, mask_d, n, acc, st)
+                                   : launch_stats<double, float>(dose_d, mask_d, n, acc, st);
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, acc, sizeof(host), cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(acc, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return set_error(PVD_ERR_CUDA, std::string("pvd_roi_stats: ") + cudaGetErrorString(e));
+  out->count = (long long)host[2];
+  out->nonfinite = (long long)host[3];
+  if (host[2] > host[3]) {
+    out->min = key_to_value(host[0], dose_dtype);
+    out->max = key_to_value(host[1], dose_dtype);
+  }
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_histogram(const void* dose_d, int dose_dtype, const void* mask_d, int mask_dtype, long long n,
+                                    const void* edges_d, int bins, long long* counts_d, pvd_stream stream) {
+  if (!dose_d || !edges_d || !counts_d) return set_error(PVD_ERR_ARG, "pvd_histogram: null argument");
+  if (n < 0 || bins < 1) return set_error(PVD_ERR_ARG, "pvd_histogram: need n >= 0 and bins >= 1");
+  if (!dtypes_ok(dose_dtype, mask_dtype))
+    return set_error(PVD_ERR_ARG, "pvd_histogram: dose must be PVD_DTYPE_F32/F64, mask PVD_DTYPE_U8/F32");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(counts_d, 0, sizeof(long long) * (size_t)bins, st);
+  if (e != cudaSuccess) return set_error(PVD_ERR_CUDA, std::string("pvd_histogram: ") + cudaGetErrorString(e));
+  if (n == 0) return PVD_OK;
+  unsigned long long* c = (unsigned long long*)counts_d;
+  if (dose_dtype == PVD_DTYPE_F32)
+    (mask_dtype == PVD_DTYPE_U8) ? launch_hist<float, unsigned char>(dose_d, mask_d, n, edges_d, bins, c, st)
+                                 : launch_hist<float, float>(dose_d, mask_d, n, edges_d, bins, c, st);
+  else
+    (mask_dtype == PVD_DTYPE_U8) ? launch_hist<double, unsigned char>(dose_d, mask_d, n, edges_d, bins, c, st)
+                                 : launch_hist<double, float>(dose_d, mask_d, n, edges_d, bins, c, st);
+  PVD_LAUNCH_CHECK("k_histogram");
+  return PVD_OK;
+}

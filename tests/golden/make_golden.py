@@ -19,6 +19,7 @@ Recorded (reference file:line in parentheses):
   fit_*    TimeCurveFitting.fit_time_activity_curve (time_integration/curve_fitting.py:19-84)
   adv_*    TimeCurveFitting.fit_time_activity_curve_advanced (curve_fitting.py:112-219)
   y90k_*   Y90KernelGenerator.generate_kernel (data/dose_kernels/y90_kernel.py:20-55)
+  dvh_*    calculate_dvh (core/utils.py:233-262)
 
 Run:  python tests/golden/make_golden.py
 """
@@ -165,6 +166,26 @@ def main():
     for tissue in ["water", "bone"]:
         kk = Y90KernelGenerator(tissue).generate_kernel(2.0, (15, 15, 15))
         g[f"y90k_{tissue}"] = kk
+
+    # ---- dose-volume histograms (own generator: the vectors above stay as they were) ----
+    from pyvoxeldosimetry.core.utils import calculate_dvh
+    r2 = np.random.default_rng(233)
+    dvh_cases = {
+        "f32_bool": ((r2.random((10, 12, 14)) * 40.0).astype(np.float32),
+                     r2.random((10, 12, 14)) > 0.4, 50),
+        # doses on a 0.25 Gy grid: many values exactly on bin edges
+        "f32_ties": ((np.round(r2.random((9, 11, 13)) * 100.0) / 4.0).astype(np.float32),
+                     (r2.random((9, 11, 13)) > 0.3).astype(np.uint8), 100),
+        "f64_const": (np.full((6, 7, 8), 3.25), r2.random((6, 7, 8)).astype(np.float32) - 0.5, 7),
+        "f64_many_bins": (r2.gamma(2.0, 5.0, (16, 16, 16)), r2.random((16, 16, 16)) > 0.1, 20000),
+    }
+    for name, (dose, mask, nb) in dvh_cases.items():
+        e, c = calculate_dvh(dose, mask, bins=nb)
+        g[f"dvh_{name}_dose"] = dose
+        g[f"dvh_{name}_mask"] = mask
+        g[f"dvh_{name}_bins"] = np.array(nb)
+        g[f"dvh_{name}_edges"] = e
+        g[f"dvh_{name}_cum"] = c
 
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")

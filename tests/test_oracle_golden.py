@@ -62,3 +62,39 @@ def test_advanced_fit_is_reference(golden, model, name):
     key = name.replace("-", "_")
     np.testing.assert_allclose(p, golden[f"adv_{key}_params"], rtol=1e-12)
     np.testing.assert_allclose(auc, golden[f"adv_{key}_auc"], rtol=1e-12)
+
+
+DVH_CASES = ["f32_bool", "f32_ties", "f64_const", "f64_many_bins"]
+
+
+@pytest.mark.parametrize("name", DVH_CASES)
+def test_dvh_is_reference(golden, name):
+    from oracle import dvh as od
+    e, c = od.calculate_dvh(golden[f"dvh_{name}_dose"], golden[f"dvh_{name}_mask"], int(golden[f"dvh_{name}_bins"]))
+    assert e.dtype == golden[f"dvh_{name}_edges"].dtype
+    np.testing.assert_array_equal(e, golden[f"dvh_{name}_edges"])
+    np.testing.assert_array_equal(c, golden[f"dvh_{name}_cum"])
+
+
+def _adversarial(dtype, rng):
+    """Values on, just below and just above bin edges, ties, a constant run, negatives."""
+    base = rng.gamma(2.0, 3.0, 4000).astype(dtype)
+    edges = np.linspace(base.min(), base.max(), 101, dtype=dtype)
+    on = rng.choice(edges, 2000)
+    below = np.nextafter(on, dtype(-np.inf))
+    above = np.nextafter(on, dtype(np.inf))
+    return np.concatenate([base, on, below, above, np.full(50, on[0]), -base[:300]]).astype(dtype)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("bins", [1, 7, 100, 1000, 20000])
+def test_restated_numpy_binning_equals_np_histogram(dtype, bins):
+    """The GPU histogram follows this step-by-step restatement of numpy's uniform-bin
+    arithmetic; it must give np.histogram's counts and edges exactly."""
+    from oracle import dvh as od
+    rng = np.random.default_rng(bins)
+    for a in (_adversarial(dtype, rng), np.full(33, dtype(2.5)), rng.random(5000).astype(dtype) * 1e-30):
+        h, e = np.histogram(a, bins=bins)
+        h2, e2 = od.numpy_uniform_bins(a, bins)
+        np.testing.assert_array_equal(e2, e)
+        np.testing.assert_array_equal(h2, h)
