@@ -338,6 +338,36 @@ def measure_dvh(device, shape=(256, 256, 256), bins=1000, reps=5):
                         "whole call (two device passes, two small host round trips)"}
 
 
+def measure_resample(device, shape=(256, 256, 256), reps=5):
+    """Cubic B-spline resampling 1.5 mm -> 2.0 mm and 2.0 mm -> 1.5 mm of a 256^3
+    float32 volume (resample_volume: copy, 3 prefilter passes, evaluation)."""
+    import torch
+    from pyvoxeldosimetry_gb300.core.utils import resample_volume, resampled_shape
+    g = torch.Generator(device=device).manual_seed(5)
+    vol = torch.rand(shape, generator=g, device=device)
+    res = {}
+    for name, a, b in (("down_1.5_to_2.0", 1.5, 2.0), ("up_2.0_to_1.5", 2.0, 1.5)):
+        resample_volume(vol, (a,) * 3, (b,) * 3)
+        ms = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            resample_volume(vol, (a,) * 3, (b,) * 3)
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        t = float(np.median(ms))
+        m = int(np.prod(resampled_shape(shape, (a,) * 3, (b,) * 3)))
+        n = int(np.prod(shape))
+        # clone 8 B, prefilter 3 x 8 B per input voxel; evaluation reads the coefficients
+        # (4 B per input voxel at best) and writes 4 B per output voxel
+        peak, _ = load_peaks()
+        bytes_ = 36 * n + 4 * m
+        res[name] = {"ms": t, "out_gvox_s": m / (t / 1e3) / 1e9, "hbm_frac": bytes_ / (t / 1e3) / 1e9 / peak}
+    return {"value": res["down_1.5_to_2.0"]["out_gvox_s"], "unit": "Gvoxel/s (output)", "cases": res,
+            "workload": "resample_volume order 3, 256^3 float32, whole call"}
+
+
 def run_only(args, device):
     """One sub-measurement alone (a bounded case to profile), printed as its own JSON line."""
     small = args.small
@@ -345,6 +375,8 @@ def run_only(args, device):
         r = measure_mc(device, n_hist=1_000_000 if small else 10_000_000)
     elif args.only == "fit":
         r = measure_fit(device, shape=(128, 128, 128) if small else (256, 256, 256))
+    elif args.only == "resample":
+        r = measure_resample(device, shape=(128, 128, 128) if small else (256, 256, 256))
     elif args.only == "dvh":
         r = measure_dvh(device, shape=(128, 128, 128) if small else (256, 256, 256))
     elif args.only == "vpfit":
@@ -432,7 +464,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the MC, fit and batch sub-measurements")
     ap.add_argument("--batch-volumes", type=int, default=8,
                     help="volumes of the 64-volume seeded uneven batch to run in the batch sub-measurement")
-    ap.add_argument("--only", choices=["mc", "fit", "vpfit", "batch", "dvh"],
+    ap.add_argument("--only", choices=["mc", "fit", "vpfit", "batch", "dvh", "resample"],
                     help="run one sub-measurement alone and print it (no contract line)")
     ap.add_argument("--small", action="store_true", help="with --only: a bounded case for profiling")
     args = ap.parse_args()
@@ -569,6 +601,7 @@ def main():
         line["tac_fit_vp"] = measure_vp_fit(device)
         line["batch"] = measure_batch(device, args.batch_volumes)
         line["dvh"] = measure_dvh(device)
+        line["resample"] = measure_resample(device)
 
     if rank == 0 and not args.no_cpu_baseline:
         ks = reference_kernels(wl)

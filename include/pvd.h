@@ -397,6 +397,31 @@ pvd_status pvd_histogram(const void* dose_d, int dose_dtype, const void* mask_d,
                          const void* edges_d, int bins, long long* counts_d, pvd_stream stream);
 
 /* ------------------------------------------------------------------------ */
+/* Resampling                                                                 */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces the activity resampling the reference leaves as a stub on the
+ * convolution path (_resample_activity, core/kernel_convolution.py:108-114)
+ * and the order-3 spline resampling of resample_dose_map (core/utils.py:193-231,
+ * through nibabel).  The spline is scipy.ndimage's interpolating cubic
+ * B-spline with mirror boundaries (map_coordinates(order=3, mode='mirror')). */
+
+/* coef_d = the cubic B-spline coefficients (mirror boundaries) of the float32
+ * volume src_d [n0][n1][n2]; scratch_d is a third buffer of the same size.
+ * All three are device buffers and must be distinct.  Enqueued on `stream`. */
+pvd_status pvd_bspline_prefilter(const float* src_d, float* coef_d, float* scratch_d, int n0, int n1, int n2,
+                                 pvd_stream stream);
+
+/* out[j0][j1][j2] = value_scale * f(u), u_a = j_a * step[a] + origin[a] in input
+ * voxel units (voxel centres at integers), f the cubic B-spline with the
+ * coefficients src_d (order 3, after pvd_bspline_prefilter) or the trilinear
+ * interpolant of src_d (order 1), both extended by mirroring.  step / origin:
+ * host double[3].  Enqueued on `stream`. */
+pvd_status pvd_resample(const float* src_d, int n0, int n1, int n2, float* out_d, int m0, int m1, int m2,
+                        const double* step, const double* origin, int order, float value_scale,
+                        pvd_stream stream);
+
+/* ------------------------------------------------------------------------ */
 /* Misc                                                                       */
 /* ------------------------------------------------------------------------ */
 

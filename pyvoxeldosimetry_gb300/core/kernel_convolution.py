@@ -17,8 +17,12 @@ Differences from the reference, each deliberate:
     resampling is needed (the reference's ``_resample_activity`` is a stub that
     returns None, kernel_convolution.py:108-114).  An explicit kernel
     (``config['kernel']`` or assigning ``calculator.kernel``) or
-    ``kernel_profile='reference'`` keeps the reference rule that the activity
-    voxel size must equal ``kernel_resolution``;
+    ``kernel_profile='reference'`` is defined at ``kernel_resolution``: an
+    activity at another voxel size is resampled to that grid on the GPU
+    (cubic B-spline, total activity conserved; ``config['resample_order']`` 1
+    for trilinear), convolved there, and the dose resampled back to the
+    activity's grid (``config['resample_output'] = 'kernel'`` returns the
+    kernel-grid dose, which is what the reference's stub was meant to feed);
   * an optional density map gives the density-scaled dose D/rho;
   * the multi-timepoint trapezoid runs as ONE convolution of the trapezoid-
     weighted activity (identical by linearity) with the weighting fused into
@@ -90,10 +94,8 @@ class KernelConvolutionCalculator(DosimetryCalculator):
     def _kernel_specs(self, voxel_size) -> List[Tuple[np.ndarray, float, bool]]:
         """(kernel FP64, scale, normalise-on-GPU) per nuclide."""
         vs = tuple(float(v) for v in voxel_size)
-        if self.kernel is not None or self.kernel_profile == "reference":
-            if vs != (float(self.kernel_resolution),) * 3:
-                raise ValueError(f"voxel_size {vs} differs from kernel_resolution {self.kernel_resolution}: "
-                                 "activity resampling is not implemented for explicit/reference kernels")
+        if self._fixed_grid() and vs != (float(self.kernel_resolution),) * 3:
+            raise ValueError(f"voxel_size {vs} differs from kernel_resolution {self.kernel_resolution}")
         if self.kernel is not None:
             ks = self.kernel if isinstance(self.kernel, (list, tuple)) else [self.kernel] * len(self.nuclides)
             if len(ks) != len(self.nuclides):
@@ -131,10 +133,43 @@ class KernelConvolutionCalculator(DosimetryCalculator):
         self._plan, self._plan_key = plan, key
         return plan
 
+    def _fixed_grid(self) -> bool:
+        """Kernels defined at kernel_resolution (explicit or the reference generators)."""
+        return self.kernel is not None or self.kernel_profile == "reference"
+
+    def _run_resampled(self, activity, voxel_size, density, weights, out_scale, out):
+        """Activity (and density) resampled to the kernel grid, convolved there, the
+        dose resampled back to the activity's grid (or returned on the kernel grid)."""
+        from .utils import resample_volume
+        kr = (float(self.kernel_resolution),) * 3
+        vs = tuple(float(v) for v in voxel_size)
+        order = int(self.config.get("resample_order", 3))
+        acts = activity if weights is not None else [activity]
+        kind = _io.kind_of(acts[0])
+        device = _require_cuda(self.device if self.device is not None else
+                               (acts[0].device if kind == _io.CUDA_TENSOR else None))
+        shape = tuple(acts[0].shape)
+        with torch.cuda.device(device):
+            dev_acts = [resample_volume(_io.to_device(a, device, "activity"), vs, kr, order=order,
+                                        conserve_total=True) for a in acts]
+            rho = None
+            if density is not None:
+                if tuple(density.shape) != shape:
+                    raise ValueError("density map must have the activity map's shape")
+                rho = resample_volume(_io.to_device(density, device, "density"), vs, kr, order=1)
+            res = self._run(dev_acts if weights is not None else dev_acts[0], kr, rho, weights, out_scale, None)
+            if self.config.get("resample_output", "input") != "kernel":
+                maps = res if not isinstance(self.radionuclide, str) else res[None]
+                back = torch.stack([resample_volume(mp, kr, vs, order=order, output_shape=shape) for mp in maps])
+                res = back if not isinstance(self.radionuclide, str) else back[0]
+            return _io.from_device(res, kind, out)
+
     # -- public API -------------------------------------------------------------
     def _run(self, activity, voxel_size, density, weights, out_scale, out):
         if len(voxel_size) != 3:
             raise ValueError("voxel_size must be a tuple of length 3.")
+        if self._fixed_grid() and tuple(float(v) for v in voxel_size) != (float(self.kernel_resolution),) * 3:
+            return self._run_resampled(activity, voxel_size, density, weights, out_scale, out)
         acts = activity if weights is not None else [activity]
         kind = _io.kind_of(acts[0])
         device = _require_cuda(self.device if self.device is not None else

@@ -292,3 +292,68 @@ def load_dose_map(filename):
                     pass
             pos += esize
     return data, metadata
+
+
+# ---------------------------------------------------------------------------
+# Resampling (core/utils.py:193-231, core/kernel_convolution.py:108-114)
+# ---------------------------------------------------------------------------
+def resampled_shape(shape, input_spacing, output_spacing) -> Tuple[int, ...]:
+    """ceil(shape * input_spacing / output_spacing) per axis (the reference's output
+    shape, core/utils.py:218-220), ignoring a rounding excess below 1e-9 voxel."""
+    return tuple(int(np.ceil(n * float(a) / float(b) - 1e-9)) for n, a, b in zip(shape, input_spacing, output_spacing))
+
+
+def resample_volume(volume, input_spacing, output_spacing, order: int = 3, conserve_total: bool = False,
+                    output_shape=None, device=None):
+    """Resample a 3-D volume from ``input_spacing`` to ``output_spacing`` (mm) on the GPU.
+
+    Both grids share the volume's outer corner: input voxel i covers
+    [i, i+1) * input_spacing, output voxel j is sampled at its centre
+    (j + 0.5) * output_spacing.  ``order`` 3 is the interpolating cubic B-spline
+    with mirror boundaries (scipy.ndimage.map_coordinates(order=3, mode='mirror')),
+    1 trilinear.  ``conserve_total`` multiplies by the voxel-volume ratio, for
+    extensive quantities such as activity per voxel (Bq): the total is then
+    preserved to interpolation accuracy.  The output shape defaults to
+    ``resampled_shape``.  Returns the caller's array kind.
+    """
+    from .. import _io
+    if order not in (1, 3):
+        raise ValueError("order must be 1 (trilinear) or 3 (cubic B-spline)")
+    kind = _io.kind_of(volume)
+    dev = _require_cuda(device if device is not None else (volume.device if kind == _io.CUDA_TENSOR else None))
+    shape = tuple(volume.shape)
+    if len(shape) != 3:
+        raise ValueError("volume must be 3-D")
+    inp = tuple(float(x) for x in input_spacing)
+    outp = tuple(float(x) for x in output_spacing)
+    if len(inp) != 3 or len(outp) != 3 or min(inp + outp) <= 0:
+        raise ValueError("spacings must be three positive values")
+    m = tuple(int(x) for x in (output_shape or resampled_shape(shape, inp, outp)))
+    step = [b / a for a, b in zip(inp, outp)]
+    origin = [0.5 * s - 0.5 for s in step]
+    scale = float(np.prod(outp) / np.prod(inp)) if conserve_total else 1.0
+    lib = N.load()
+    with torch.cuda.device(dev):
+        src = _io.to_device(volume, dev, "volume")
+        sh = torch.cuda.current_stream(dev).cuda_stream
+        if order == 3:
+            coef = torch.empty_like(src)
+            scratch = torch.empty_like(src)
+            N.check(lib.pvd_bspline_prefilter(src.data_ptr(), coef.data_ptr(), scratch.data_ptr(), *shape, sh))
+            del scratch
+            src = coef
+        out = torch.empty(m, dtype=torch.float32, device=dev)
+        N.check(lib.pvd_resample(src.data_ptr(), *shape, out.data_ptr(), *m, (C.c_double * 3)(*step),
+                                 (C.c_double * 3)(*origin), order, scale, sh))
+        return _io.from_device(out, kind)
+
+
+def resample_dose_map(dose_map, input_spacing, output_spacing, order: int = 3):
+    """The reference's resample_dose_map (core/utils.py:193-231): order-3 spline
+    resampling to ``output_spacing``; returns (resampled, affine).  The input
+    affine is the reference's diag(input_spacing) (voxel 0 at the origin); the
+    returned affine places the output voxels on the same physical extent."""
+    res = resample_volume(dose_map, input_spacing, output_spacing, order=order)
+    aff = np.diag([float(x) for x in output_spacing] + [1.0])
+    aff[:3, 3] = [0.5 * (float(b) - float(a)) for a, b in zip(input_spacing, output_spacing)]
+    return res, aff
