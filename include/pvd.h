@@ -422,6 +422,38 @@ pvd_status pvd_resample(const float* src_d, int n0, int n1, int n2, float* out_d
                         pvd_stream stream);
 
 /* ------------------------------------------------------------------------ */
+/* Dose-point kernels                                                         */
+/* ------------------------------------------------------------------------ */
+
+/* The reference generates its kernels in numpy on the CPU
+ * (data/dose_kernels/kernel_factory.py:37-75 and the *_kernel.py generators);
+ * here a kernel is a sum of radial terms evaluated in FP64 on the device:
+ *   PVD_TERM_COLE    weight (1 - r/p1)^2 exp(-2 r/p1) for r <= p1 (beta, positron)
+ *   PVD_TERM_PHOTON  weight exp(-p1 r / 10) / (4 pi r^2), p1 = mu in 1/cm
+ *   PVD_TERM_ALPHA   weight (1 - (r/p1)^p2) exp(-p3 r/p1) for r <= p1
+ *   PVD_TERM_EXP_R2  weight exp(-r/p1) / r^2
+ * with r in mm from the centre voxel (k/2 on each axis).  At r = 0 the PHOTON
+ * and EXP_R2 terms use the radius of the sphere of the voxel's volume
+ * (PVD_CENTER_R0), 0 (PVD_CENTER_ZERO) or NaN (PVD_CENTER_NAN, the reference's
+ * 0 * inf for Y-90 and Ga-68). */
+#define PVD_MAX_RADIAL_TERMS 16
+enum { PVD_TERM_COLE = 0, PVD_TERM_PHOTON = 1, PVD_TERM_ALPHA = 2, PVD_TERM_EXP_R2 = 3 };
+enum { PVD_CENTER_R0 = 0, PVD_CENTER_ZERO = 1, PVD_CENTER_NAN = 2 };
+typedef struct {
+  int type;       /* PVD_TERM_* */
+  int center;     /* PVD_CENTER_*: value at r = 0 of PHOTON and EXP_R2 terms */
+  double weight;
+  double p1;      /* COLE / ALPHA: range (mm); PHOTON: mu (1/cm); EXP_R2: decay length (mm) */
+  double p2;      /* ALPHA: exponent of r / range */
+  double p3;      /* ALPHA: decay constant */
+} pvd_radial_term;
+
+/* out_d (device float64 [k0][k1][k2]) = scale * sum of the terms; voxel_mm: host
+ * double[3].  Enqueued on `stream`. */
+pvd_status pvd_radial_kernel(const pvd_radial_term* terms, int n_terms, double scale, int k0, int k1, int k2,
+                             const double* voxel_mm, double* out_d, pvd_stream stream);
+
+/* ------------------------------------------------------------------------ */
 /* Misc                                                                       */
 /* ------------------------------------------------------------------------ */
 

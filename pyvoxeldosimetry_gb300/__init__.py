@@ -14,6 +14,9 @@ from .core.activity_sampler import ActivitySampler
 from .core.dose_calculator import DoseCalculator, DoseCalculationResult
 from .core.monte_carlo import MonteCarloCalculator
 from .time_integration.curve_fitting import TimeCurveFitting
+from .core.utils import calculate_dvh, load_dose_map, resample_dose_map, resample_volume, save_dose_map
+from .data.dose_kernels import KernelFactory
+from .batch import BatchDoseCalculator
 
 __all__ = [
     "DosimetryCalculator",
@@ -23,4 +26,11 @@ __all__ = [
     "DoseCalculationResult",
     "MonteCarloCalculator",
     "TimeCurveFitting",
+    "calculate_dvh",
+    "save_dose_map",
+    "load_dose_map",
+    "resample_dose_map",
+    "resample_volume",
+    "KernelFactory",
+    "BatchDoseCalculator",
 ]

@@ -44,6 +44,7 @@ EXPORTED_SYMBOLS = [
     "pvd_batch_execute", "pvd_batch_create", "pvd_batch_run", "pvd_batch_destroy",
     "pvd_roi_stats", "pvd_histogram",
     "pvd_bspline_prefilter", "pvd_resample",
+    "pvd_radial_kernel",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
 ]
 
@@ -83,6 +84,16 @@ class BatchItem(C.Structure):
 
 class RoiStats(C.Structure):
     _fields_ = [("min", C.c_double), ("max", C.c_double), ("count", C.c_longlong), ("nonfinite", C.c_longlong)]
+
+
+class RadialTerm(C.Structure):
+    _fields_ = [("type", C.c_int), ("center", C.c_int), ("weight", C.c_double), ("p1", C.c_double),
+                ("p2", C.c_double), ("p3", C.c_double)]
+
+
+PVD_TERM_COLE, PVD_TERM_PHOTON, PVD_TERM_ALPHA, PVD_TERM_EXP_R2 = 0, 1, 2, 3
+PVD_CENTER_R0, PVD_CENTER_ZERO, PVD_CENTER_NAN = 0, 1, 2
+PVD_MAX_RADIAL_TERMS = 16
 
 
 class PlanInfo(C.Structure):
@@ -142,6 +153,7 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_roi_stats": (st, [vp, i, vp, i, C.c_longlong, C.POINTER(RoiStats), vp]),
         "pvd_histogram": (st, [vp, i, vp, i, C.c_longlong, vp, i, vp, vp]),
         "pvd_bspline_prefilter": (st, [vp, vp, vp, i, i, i, vp]),
+        "pvd_radial_kernel": (st, [C.POINTER(RadialTerm), i, d, i, i, i, C.POINTER(C.c_double), vp, vp]),
         "pvd_resample": (st, [vp, i, i, i, vp, i, i, i, C.POINTER(C.c_double), C.POINTER(C.c_double), i, f, vp]),
         "pvd_last_error": (st, [C.c_char_p, C.c_size_t]),
         "pvd_version": (i, []),

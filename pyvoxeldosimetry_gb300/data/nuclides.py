@@ -15,9 +15,8 @@ Kernel profiles:
                 the others; the centre voxel uses the radius of the sphere of equal
                 volume r0 = (3 dV / 4 pi)^(1/3).  Normalised (on the GPU, FP64) so the
                 kernel sums to 1, then scaled to Gy/(Bq s) by the mean beta energy.
-  "reference" : restatement of the reference generators
-                (data/dose_kernels/y90_kernel.py:20-140, lu177_kernel.py:52-184) with the
-                r = 0 singularity of the photon term replaced by r0 (the reference
+  "reference" : the reference generators' kernels (data.dose_kernels, GPU FP64) with the
+                r = 0 singularity of the photon terms replaced by r0 (the reference
                 produces NaN there, y90_kernel.py:134-138).
 """
 from __future__ import annotations
@@ -62,15 +61,9 @@ NUCLIDES = {
     "F18": Nuclide("F18", 1.8295, 0.250, 0.634, 2.4, 6.0),
     "Ga68": Nuclide("Ga68", 1.128, 0.836, 1.899, 9.0, 12.0),
     "Tb161": Nuclide("Tb161", 165.432, 0.154, 0.593, 1.8, 6.0),
-}
-
-# Tissue properties used by the reference generators (y90_kernel.py:57-91, lu177_kernel.py:88-127).
-TISSUES = {
-    "water": dict(density=1.0, effective_Z=7.42, stopping_power_ratio=1.0, mu_by_rho=0.096, scale=1.0),
-    "lung": dict(density=0.26, effective_Z=7.41, stopping_power_ratio=1.04, mu_by_rho=0.095, scale=1.04),
-    "soft_tissue": dict(density=1.04, effective_Z=7.46, stopping_power_ratio=1.04, mu_by_rho=0.097, scale=1.04),
-    "bone": dict(density=1.85, effective_Z=13.8, stopping_power_ratio=1.15, mu_by_rho=0.110, scale=1.15),
-    "iodine_contrast": dict(density=1.30, effective_Z=53.0, stopping_power_ratio=1.12, mu_by_rho=0.245, scale=1.12),
+    # alpha emitter (data/dose_kernels/Ac225/Ac225.json): kernels only from the reference
+    # generator's form (kernel_profile='reference'); no beta terms
+    "Ac225": Nuclide("Ac225", 240.0, 0.0, 0.0, 0.0, 5.0, extra={"alpha": True}),
 }
 
 Y90_LAMBDA_MM = 1.8
@@ -113,6 +106,8 @@ def equal_volume_radius(voxel_size) -> float:
 
 def analytic_lambda_mm(symbol: str) -> float:
     nuc = get_nuclide(symbol)
+    if nuc.extra.get("alpha"):
+        raise ValueError(f"{symbol} is an alpha emitter: no analytic beta profile; use kernel_profile='reference'")
     return Y90_LAMBDA_MM * nuc.beta_csda_range_mm / NUCLIDES["Y90"].beta_csda_range_mm
 
 
@@ -129,57 +124,18 @@ def gy_per_bq_s_scale(symbol: str, voxel_size, water_density: float = 1.0) -> fl
     """Mean beta energy per decay deposited in one voxel of water, in Gy per (Bq s):
     E_mean [MeV] * 1.602176634e-13 [J/MeV] / (rho * dV [mm^3] * 1e-6 [kg / (g/cc mm^3)])."""
     v = _vox3(voxel_size)
-    return get_nuclide(symbol).beta_mean_mev * JOULE_PER_MEV / (water_density * v[0] * v[1] * v[2] * 1e-6)
-
-
-# --------------------------------------------------------------------------
-# restatement of the reference generators
-# --------------------------------------------------------------------------
-def _beta_cole(r, e_max, coef, tissue):
-    """(1 - r/R)^2 exp(-2 r/R) * rho * SPR for r <= R, R = coef * Emax^1.5 / rho / SPR
-    (y90_kernel.py:93-117 with coef 11; lu177_kernel.py:129-154 with coef 5)."""
-    rho, spr = tissue["density"], tissue["stopping_power_ratio"]
-    rng = coef * e_max ** 1.5 * (1.0 / rho) * (1.0 / spr)
-    out = np.zeros_like(r)
-    m = r <= rng
-    out[m] = (1 - r[m] / rng) ** 2 * np.exp(-2 * r[m] / rng) * rho * spr
-    return out
+    nuc = get_nuclide(symbol)
+    if nuc.extra.get("alpha"):
+        raise ValueError(f"{symbol} is an alpha emitter: no analytic beta profile; use kernel_profile='reference'")
+    return nuc.beta_mean_mev * JOULE_PER_MEV / (water_density * v[0] * v[1] * v[2] * 1e-6)
 
 
 def reference_profile(symbol: str, tissue: str, voxel_size: float, shape, fix_r0: bool = True) -> np.ndarray:
-    """The reference's Y-90 / Lu-177 generator kernels (isotropic voxel).
-
-    Y-90: Cole beta term + bremsstrahlung 0.015 (Z/7.42)^2 rho exp(-mu r/10)/(4 pi r^2),
-    mu = 0.096 rho /cm, times the tissue scaling factor (y90_kernel.py:20-55, 119-161).
-    Lu-177: abundance-weighted Cole terms (5 Emax^1.5 range) + gamma lines
-    I exp(-mu r/10)/(4 pi r^2), mu = rho (mu/rho) (0.2/E)^3.2 (lu177_kernel.py:52-86, 156-184).
-    With ``fix_r0`` the photon terms use r0 at the centre voxel instead of the
-    reference's 0 * inf = NaN.
-    """
-    t = TISSUES.get(tissue, TISSUES["water"])
-    r = radius_grid(tuple(shape), voxel_size)
-    rc = np.where(r == 0.0, equal_volume_radius(voxel_size), r) if fix_r0 else r
-    nuc = get_nuclide(symbol)
-    with np.errstate(divide="ignore", invalid="ignore"):
-        if symbol == "Y90":
-            k = _beta_cole(r, nuc.beta_max_mev, 11.0, t)
-            mu = 0.096 * (t["density"] / 1.0)
-            rel_yield = (t["effective_Z"] / 7.42) ** 2
-            brems = 0.015 * rel_yield * t["density"] * np.exp(-mu * rc / 10) / (4 * np.pi * rc ** 2)
-            if not fix_r0:
-                brems = brems * (r > 0)
-            k = k + brems
-            k = k * t["scale"]
-        elif symbol == "Lu177":
-            k = np.zeros_like(r)
-            for e_max, ab in nuc.beta_branches:
-                k += ab * _beta_cole(r, e_max, 5.0, t)
-            for e_g, inten in ((0.208, 0.111), (0.113, 0.062)):  # dose_kernels/Lu177/Lu177.json:23-26
-                mu = t["density"] * t["mu_by_rho"] * (0.2 / e_g) ** 3.2
-                g = inten * np.exp(-mu * rc / 10) / (4 * np.pi * rc ** 2)
-                if not fix_r0:
-                    g = np.where(r > 0, g, 0.0)
-                k += g
-        else:
-            raise ValueError(f"no reference generator for {symbol} (the reference ships Y90 and Lu177 only)")
-    return k
+    """The reference generator's kernel for ``symbol`` (Y90, Lu177, Ga68, F18, Tb161,
+    Ac225), computed on the GPU by the kernel library (``data.dose_kernels``).  With
+    ``fix_r0`` the photon terms use the radius of the sphere of the voxel's volume at
+    the centre voxel instead of the reference's NaN (0 * inf) or 0."""
+    from .dose_kernels import generate_kernel
+    if symbol not in ("Y90", "Lu177", "Ga68", "F18", "Tb161", "Ac225"):
+        raise ValueError(f"no reference generator for {symbol}")
+    return generate_kernel(symbol, tissue, voxel_size, tuple(shape), reference_r0=not fix_r0)

@@ -20,6 +20,12 @@ Recorded (reference file:line in parentheses):
   adv_*    TimeCurveFitting.fit_time_activity_curve_advanced (curve_fitting.py:112-219)
   y90k_*   Y90KernelGenerator.generate_kernel (data/dose_kernels/y90_kernel.py:20-55)
   dvh_*    calculate_dvh (core/utils.py:233-262)
+  kgen_*   Ga68KernelGenerator.generate_kernel (data/dose_kernels/ga68_kernel.py:19-106),
+           Lu177KernelGenerator.generate_kernel (lu177_kernel.py:52-184), and the
+           alpha / gamma terms of Ac225KernelGenerator (ac225_kernel.py:140-184; its
+           generate_kernel calls a method the class does not define).  The generators'
+           JSON files carry // comments, which json.load rejects; they are read with
+           the comments stripped.
 
 Run:  python tests/golden/make_golden.py
 """
@@ -61,6 +67,25 @@ def _install_stubs():
         sys.modules[name] = _Stub(name)
     if not hasattr(np, "trapz"):
         np.trapz = np.trapezoid
+
+
+def strip_json_comments(text: str) -> str:
+    """Drop // comments outside string literals (the reference's kernel JSON files use them)."""
+    out = []
+    for line in text.splitlines():
+        in_str, esc, cut = False, False, len(line)
+        for i, ch in enumerate(line):
+            if esc:
+                esc = False
+            elif ch == "\\":
+                esc = True
+            elif ch == '"':
+                in_str = not in_str
+            elif not in_str and line.startswith("//", i):
+                cut = i
+                break
+        out.append(line[:cut])
+    return "\n".join(out)
 
 
 def main():
@@ -186,6 +211,32 @@ def main():
         g[f"dvh_{name}_bins"] = np.array(nb)
         g[f"dvh_{name}_edges"] = e
         g[f"dvh_{name}_cum"] = c
+
+    # ---- kernel generators (configs read with the // comments stripped) ----
+    import json
+    from pyvoxeldosimetry.data.dose_kernels import base_kernel
+    base_kernel.BaseKernelGenerator._load_config = lambda self, path: json.loads(
+        strip_json_comments(Path(path).read_text()))
+    from pyvoxeldosimetry.data.dose_kernels.ac225_kernel import Ac225KernelGenerator
+    from pyvoxeldosimetry.data.dose_kernels.ga68_kernel import Ga68KernelGenerator
+    from pyvoxeldosimetry.data.dose_kernels.lu177_kernel import Lu177KernelGenerator
+    for tissue in ["water", "bone", "lung"]:
+        g[f"kgen_ga68_{tissue}"] = Ga68KernelGenerator(tissue).generate_kernel(2.0, (9, 9, 9))
+    for tissue in ["water", "bone"]:
+        g[f"kgen_lu177_{tissue}"] = Lu177KernelGenerator(tissue).generate_kernel(1.5, (11, 11, 11))
+    r_alpha = np.linspace(0.0, 0.06, 49)
+    g["kgen_ac225_r_alpha"] = r_alpha
+    c = [s // 2 for s in (7, 7, 7)]
+    xx, yy, zz = np.meshgrid(*(np.arange(7) - cc for cc in c), indexing="ij")
+    r_gamma = np.sqrt(xx ** 2 + yy ** 2 + zz ** 2) * 1.0
+    g["kgen_ac225_r_gamma"] = r_gamma
+    for tissue in ["water", "bone", "lung"]:
+        ac = Ac225KernelGenerator(tissue)
+        g[f"kgen_ac225_alpha_{tissue}"] = np.stack([ac._calculate_alpha_contribution(r_alpha, a["energy"])
+                                                   for a in ac.alpha_energies])
+        g[f"kgen_ac225_gamma_{tissue}"] = np.stack([ac._calculate_gamma_contribution(r_gamma, gl["energy"],
+                                                                                     gl["intensity"])
+                                                   for gl in ac.gamma_lines])
 
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")

@@ -98,3 +98,34 @@ def test_restated_numpy_binning_equals_np_histogram(dtype, bins):
         h2, e2 = od.numpy_uniform_bins(a, bins)
         np.testing.assert_array_equal(e2, e)
         np.testing.assert_array_equal(h2, h)
+
+
+@pytest.mark.parametrize("tissue", ["water", "bone"])
+def test_y90_generator_is_reference(golden, tissue):
+    from oracle import kernels as ok
+    np.testing.assert_allclose(ok.y90(tissue, 2.0, (15, 15, 15), reference_r0=True), golden[f"y90k_{tissue}"],
+                               rtol=1e-13, atol=0, equal_nan=True)
+
+
+@pytest.mark.parametrize("tissue", ["water", "bone", "lung"])
+def test_ga68_generator_is_reference(golden, tissue):
+    from oracle import kernels as ok
+    np.testing.assert_allclose(ok.ga68(tissue, 2.0, (9, 9, 9), reference_r0=True), golden[f"kgen_ga68_{tissue}"],
+                               rtol=1e-13, atol=0, equal_nan=True)
+
+
+@pytest.mark.parametrize("tissue", ["water", "bone"])
+def test_lu177_generator_is_reference(golden, tissue):
+    from oracle import kernels as ok
+    np.testing.assert_allclose(ok.lu177(tissue, 1.5, (11, 11, 11), reference_r0=True),
+                               golden[f"kgen_lu177_{tissue}"], rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("tissue", ["water", "bone", "lung"])
+def test_ac225_terms_are_reference(golden, tissue):
+    from oracle import kernels as ok
+    ra, rg = golden["kgen_ac225_r_alpha"], golden["kgen_ac225_r_gamma"]
+    al = np.stack([ok.ac225_alpha(ra, e, tissue) for e, _ in ok.AC_ALPHAS])
+    ga = np.stack([ok.ac225_gamma(rg, e, i, tissue) for e, i in ok.AC_GAMMAS])
+    np.testing.assert_allclose(al, golden[f"kgen_ac225_alpha_{tissue}"], rtol=1e-13, atol=0)
+    np.testing.assert_allclose(ga, golden[f"kgen_ac225_gamma_{tissue}"], rtol=1e-13, atol=0)
