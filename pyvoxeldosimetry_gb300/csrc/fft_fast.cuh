@@ -404,13 +404,14 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_fwd(
   if (warp < NWF) {
     for (int rr = warp; rr < nr; rr += NWF) {
       float r[NU];
-      if (in.n == 1) {  // one activity map (the common case): plain loads
+      if (in.n == 1) {  // one activity map (the common case): asynchronous copies, all rows in flight
         const float* src = in.p[0] + (row0 + rr) * N2;
 #pragma unroll
         for (int u = 0; u < NU; ++u) {
           const int n = 32 * u + lane;
-          r[u] = (n < N2) ? __ldg(src + n) : 0.f;
+          if (n < N2) cp_async4(chunk + rr * S + n, src + n);
         }
+        continue;
       } else {
 #pragma unroll
         for (int u = 0; u < NU; ++u) r[u] = 0.f;
@@ -431,6 +432,7 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_fwd(
       }
     }
   }
+  cp_async_wait_all();
   __syncthreads();
   const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
   float2 v[B];
@@ -497,24 +499,20 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_inv(
   const int nr = (int)min((long long)ROWS, (long long)nrows - row0);
   load_tw<L>(tw, twg, NTH);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // every row of the tile in flight at once: asynchronous copies straight into shared memory
   if (warp < NWF) {
     for (int rr = warp; rr < nr; rr += NWF) {
       const float2* src = in + (row0 + rr) * HS;
       float2* dsm = ((rr & 1) ? hb : ha) + (rr >> 1) * S2;
       constexpr int KU = (H + 31) / 32;
-      float2 r[KU];
 #pragma unroll
       for (int u = 0; u < KU; ++u) {
         const int k = 32 * u + lane;
-        if (k < H) r[u] = src[k];
-      }
-#pragma unroll
-      for (int u = 0; u < KU; ++u) {
-        const int k = 32 * u + lane;
-        if (k < H) dsm[k] = r[u];
+        if (k < H) cp_async8(dsm + k, src + k);
       }
     }
   }
+  cp_async_wait_all();
   __syncthreads();
   const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
   float2 v[B];
