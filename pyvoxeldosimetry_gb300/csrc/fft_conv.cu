@@ -44,6 +44,7 @@ constexpr int NT = 256;       // threads per CTA
 constexpr int NL = NT / TX;   // lanes per transform
 constexpr int MAX_STAGES = 16;
 constexpr int PVD_HOST_CHUNKS = 4;  // activity upload chunks overlapped with the forward passes
+constexpr int PVD_DOSE_CHUNKS = 4;  // density upload / inverse-x / dose copy-back chunks (z ranges)
 
 struct FftLen {
   int L;
@@ -459,9 +460,10 @@ struct pvd_plan {
   float* io_rho = nullptr;
   float* io_dose = nullptr;
   cudaStream_t s_h2d = nullptr, s_d2h = nullptr;
-  cudaEvent_t ev_start = nullptr, ev_rho = nullptr, ev_done = nullptr;
+  cudaEvent_t ev_start = nullptr, ev_done = nullptr;
   cudaEvent_t ev_act[PVD_HOST_CHUNKS] = {};
-  cudaEvent_t ev_dose[PVD_MAX_KERNELS] = {};
+  cudaEvent_t ev_rho[PVD_DOSE_CHUNKS] = {};
+  cudaEvent_t ev_dose[PVD_MAX_KERNELS * PVD_DOSE_CHUNKS] = {};
   std::vector<cudaEvent_t> ev_pool;
   size_t ev_used = 0;
   struct Rec { int kind; cudaEvent_t a, b; };
@@ -488,9 +490,11 @@ void plan_free(pvd_plan* p) {
   p->allocs.clear();
   if (p->s_h2d) cudaStreamDestroy(p->s_h2d);
   if (p->s_d2h) cudaStreamDestroy(p->s_d2h);
-  for (cudaEvent_t e : {p->ev_start, p->ev_rho, p->ev_done})
+  for (cudaEvent_t e : {p->ev_start, p->ev_done})
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : p->ev_act)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->ev_rho)
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : p->ev_dose)
     if (e) cudaEventDestroy(e);
@@ -942,9 +946,10 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
       k_z<<<dim3(ctiles_z, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
     PVD_LAUNCH_CHECK("z");
   }
-  const int xblocks = (nrows + rows_x - 1) / rows_x;
+  // with host buffers the inverse x pass runs in z chunks: the first slot's chunk c
+  // waits only for density chunk c, and each chunk's dose goes back as soon as it is written
+  const int dchunks = hio ? std::min(PVD_DOSE_CHUNKS, N0) : 1;
   for (int s = 0; s < p->nk; ++s) {
-    if (hio && s == 0 && hio->rho) PVD_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_rho, 0));
     {
       PassTimer t(p, 3, st);
       if (p->tma)
@@ -958,21 +963,28 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
                                                            p->tw[1]);
       PVD_LAUNCH_CHECK("y_inv");
     }
-    {
-      PassTimer t(p, 4, st);
+    PassTimer t(p, 4, st);
+    for (int c = 0; c < dchunks; ++c) {
+      const long long z0 = (long long)N0 * c / dchunks, z1 = (long long)N0 * (c + 1) / dchunks;
+      const long long r0 = z0 * N1, nr = (z1 - z0) * N1;  // rows of this chunk
+      if (nr == 0) continue;
+      if (hio && s == 0 && hio->rho) PVD_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_rho[c], 0));
+      const float2* in_c = p->buf1 + r0 * p->HS;
+      float* out_c = dose + s * vox + r0 * N2;
+      const float* rho_c = rho ? rho + r0 * N2 : nullptr;
+      const int xb = (int)((nr + rows_x - 1) / rows_x);
       if (fx)
-        fx->x_inv<<<xblocks, fx->threads, fx->smem_row, st>>>(p->buf1, dose + s * vox, rho, nrows, N2, p->HS,
-                                                               out_scale, p->tw[2]);
+        fx->x_inv<<<xb, fx->threads, fx->smem_row, st>>>(in_c, out_c, rho_c, (int)nr, N2, p->HS, out_scale, p->tw[2]);
       else
-        k_x_inv<<<xblocks, NT, p->smem_x, st>>>(p->buf1, dose + s * vox, rho, nrows, N2, p->HS, out_scale, p->f[2],
-                                               p->tw[2]);
+        k_x_inv<<<xb, NT, p->smem_x, st>>>(in_c, out_c, rho_c, (int)nr, N2, p->HS, out_scale, p->f[2], p->tw[2]);
       PVD_LAUNCH_CHECK("x_inv");
-    }
-    if (hio) {  // this slot's dose goes back while the next slot computes
-      PVD_CUDA_TRY(cudaEventRecord(p->ev_dose[s], st));
-      PVD_CUDA_TRY(cudaStreamWaitEvent(p->s_d2h, p->ev_dose[s], 0));
-      PVD_CUDA_TRY(cudaMemcpyAsync(hio->dose + s * vox, dose + s * vox, sizeof(float) * vox, cudaMemcpyDeviceToHost,
-                                   p->s_d2h));
+      if (hio) {  // this chunk goes back while the next one computes
+        cudaEvent_t ev = p->ev_dose[s * PVD_DOSE_CHUNKS + c];
+        PVD_CUDA_TRY(cudaEventRecord(ev, st));
+        PVD_CUDA_TRY(cudaStreamWaitEvent(p->s_d2h, ev, 0));
+        PVD_CUDA_TRY(cudaMemcpyAsync(hio->dose + s * vox + r0 * N2, out_c, sizeof(float) * nr * N2,
+                                     cudaMemcpyDeviceToHost, p->s_d2h));
+      }
     }
   }
   if (hio) {  // the caller's stream completes only after the last copy back
@@ -1019,7 +1031,7 @@ extern "C" pvd_status pvd_conv_execute_host(pvd_plan* p, const float* act_h, con
     PVD_CUDA_TRY(cudaStreamCreateWithFlags(&p->s_h2d, cudaStreamNonBlocking));
     PVD_CUDA_TRY(cudaStreamCreateWithFlags(&p->s_d2h, cudaStreamNonBlocking));
     PVD_CUDA_TRY(cudaEventCreateWithFlags(&p->ev_start, cudaEventDisableTiming));
-    PVD_CUDA_TRY(cudaEventCreateWithFlags(&p->ev_rho, cudaEventDisableTiming));
+    for (auto& e : p->ev_rho) PVD_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     PVD_CUDA_TRY(cudaEventCreateWithFlags(&p->ev_done, cudaEventDisableTiming));
     for (auto& e : p->ev_act) PVD_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (auto& e : p->ev_dose) PVD_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1036,9 +1048,16 @@ extern "C" pvd_status pvd_conv_execute_host(pvd_plan* p, const float* act_h, con
       PVD_CUDA_TRY(cudaMemcpyAsync(p->io_act + off, act_h + off, sizeof(float) * n, cudaMemcpyHostToDevice, p->s_h2d));
     PVD_CUDA_TRY(cudaEventRecord(p->ev_act[c], p->s_h2d));
   }
-  if (rho_h) {
-    PVD_CUDA_TRY(cudaMemcpyAsync(p->io_rho, rho_h, vb, cudaMemcpyHostToDevice, p->s_h2d));
-    PVD_CUDA_TRY(cudaEventRecord(p->ev_rho, p->s_h2d));
+  if (rho_h) {  // in the z chunks the inverse x pass consumes them in
+    const int dchunks = std::min(PVD_DOSE_CHUNKS, N0);
+    for (int c = 0; c < dchunks; ++c) {
+      const long long z0 = (long long)N0 * c / dchunks, z1 = (long long)N0 * (c + 1) / dchunks;
+      const long long off = z0 * N1 * N2, n = (z1 - z0) * N1 * N2;
+      if (n > 0)
+        PVD_CUDA_TRY(cudaMemcpyAsync(p->io_rho + off, rho_h + off, sizeof(float) * n, cudaMemcpyHostToDevice,
+                                     p->s_h2d));
+      PVD_CUDA_TRY(cudaEventRecord(p->ev_rho[c], p->s_h2d));
+    }
   }
   ActIn in;
   std::memset(&in, 0, sizeof(in));
