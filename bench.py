@@ -312,9 +312,9 @@ def measure_vp_fit(device, shape=(256, 256, 256), reps=2):
 
 
 def measure_dvh(device, shape=(256, 256, 256), bins=1000, reps=5):
-    """Dose-volume histogram (calculate_dvh): ROI statistics + histogram on the GPU,
-    edges and cumulative sum on the host; 10 algorithmic bytes per voxel (two passes
-    over a float32 dose and a uint8 mask)."""
+    """Dose-volume histogram (calculate_dvh): ROI statistics, numpy's edges and the
+    histogram on the GPU, cumulative sum on the host; 10 algorithmic bytes per voxel
+    (two passes over a float32 dose and a uint8 mask)."""
     import torch
     from pyvoxeldosimetry_gb300.core.utils import calculate_dvh
     g = torch.Generator(device=device).manual_seed(9)
@@ -335,7 +335,7 @@ def measure_dvh(device, shape=(256, 256, 256), bins=1000, reps=5):
     return {"value": nv / (t / 1e3) / 1e9, "unit": "Gvoxel/s", "ms_per_call": t, "voxels": nv, "bins": bins,
             "hbm_frac": 10.0 * nv / (t / 1e3) / 1e9 / peak,
             "workload": f"calculate_dvh, {shape[0]}x{shape[1]}x{shape[2]} float32 dose, uint8 ROI of 70 %, "
-                        "whole call (two device passes, two small host round trips)"}
+                        "whole call (statistics, edges and histogram on the device, one copy back)"}
 
 
 def measure_resample(device, shape=(256, 256, 256), reps=5):

@@ -396,6 +396,17 @@ pvd_status pvd_roi_stats(const void* dose_d, int dose_dtype, const void* mask_d,
 pvd_status pvd_histogram(const void* dose_d, int dose_dtype, const void* mask_d, int mask_dtype, long long n,
                          const void* edges_d, int bins, long long* counts_d, pvd_stream stream);
 
+/* Both steps without a host round trip: ROI statistics, numpy's edges computed on
+ * the device (np.linspace(first, last, bins + 1) restated operation for operation),
+ * counts.  result_d: device int64 [4 + bins] = [min key, max key, ROI count,
+ * non-finite ROI count, counts...]; the keys are the doses' bit patterns made
+ * order-preserving (negative values bit-inverted, positive ones with the sign bit
+ * set; float32 in the low 32 bits).  With no ROI voxel or a non-finite ROI dose
+ * nothing is counted (the caller raises, as numpy does).  edges_d: device
+ * workspace of bins + 1 values of the dose's type.  Enqueued on `stream`. */
+pvd_status pvd_dvh(const void* dose_d, int dose_dtype, const void* mask_d, int mask_dtype, long long n, int bins,
+                   void* edges_d, long long* result_d, pvd_stream stream);
+
 /* ------------------------------------------------------------------------ */
 /* Resampling                                                                 */
 /* ------------------------------------------------------------------------ */

@@ -47,3 +47,22 @@ def numpy_uniform_bins(a: np.ndarray, bins: int):
     up = (a >= edges[idx + 1]) & (idx != bins - 1)
     idx[up] += 1
     return np.bincount(idx, minlength=bins).astype(np.intp), edges
+
+
+def numpy_linspace_edges(first, last, bins):
+    """np.linspace(first, last, bins + 1) for scalar endpoints of one floating type,
+    restated (numpy/_core/function_base.py `linspace`): step = (last - first) / bins,
+    edge i = i * step + first (each operation rounded in the type), the last edge =
+    last; when the step underflows to 0, (i / bins) * (last - first) + first.  The GPU
+    computes the histogram edges this way."""
+    t = type(first)
+    delta = t(last - first)
+    step = t(delta / t(bins))
+    i = np.arange(bins + 1).astype(t)
+    if step == 0:
+        y = (i / t(bins)).astype(t) * delta
+    else:
+        y = (i * step).astype(t)
+    y = (y + first).astype(t)
+    y[-1] = last
+    return y

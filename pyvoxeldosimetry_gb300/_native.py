@@ -42,7 +42,7 @@ EXPORTED_SYMBOLS = [
     "pvd_weighted_sum", "pvd_tac_fit",
     "pvd_mc_plan_create", "pvd_mc_run", "pvd_mc_plan_destroy",
     "pvd_batch_execute", "pvd_batch_create", "pvd_batch_run", "pvd_batch_destroy",
-    "pvd_roi_stats", "pvd_histogram",
+    "pvd_roi_stats", "pvd_histogram", "pvd_dvh",
     "pvd_bspline_prefilter", "pvd_resample",
     "pvd_radial_kernel",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
@@ -152,6 +152,7 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_batch_destroy": (st, [vp]),
         "pvd_roi_stats": (st, [vp, i, vp, i, C.c_longlong, C.POINTER(RoiStats), vp]),
         "pvd_histogram": (st, [vp, i, vp, i, C.c_longlong, vp, i, vp, vp]),
+        "pvd_dvh": (st, [vp, i, vp, i, C.c_longlong, i, vp, vp, vp]),
         "pvd_bspline_prefilter": (st, [vp, vp, vp, i, i, i, vp]),
         "pvd_radial_kernel": (st, [C.POINTER(RadialTerm), i, d, i, i, i, C.POINTER(C.c_double), vp, vp]),
         "pvd_resample": (st, [vp, i, i, i, vp, i, i, i, C.POINTER(C.c_double), C.POINTER(C.c_double), i, f, vp]),

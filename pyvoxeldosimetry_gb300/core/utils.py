@@ -75,28 +75,42 @@ def calculate_dvh(dose_map, roi_mask, bins: int = 1000, device=None) -> Tuple[np
         raise ValueError("`bins` must be positive, when an integer")
     dev = _require_cuda(device)
     lib = N.load()
+    bins = int(bins)
     with torch.cuda.device(dev):
         d, dt, np_t = _dose_on_device(dose_map, dev)
         m, mt = _mask_on_device(roi_mask, dev)
-        n = d.numel()
-        st = N.RoiStats()
-        sh = torch.cuda.current_stream(dev).cuda_stream
-        N.check(lib.pvd_roi_stats(d.data_ptr(), dt, m.data_ptr(), mt, n, C.byref(st), sh))
-        if st.count == 0:
+        if d.numel() == 0:
             raise ValueError("ROI mask is empty")
-        if st.nonfinite:
-            raise ValueError("autodetected range of [nan, nan] is not finite")
-        first, last = np_t(st.min), np_t(st.max)
-        if first == last:
-            first, last = first - 0.5, last + 0.5
-        edges = np.linspace(first, last, int(bins) + 1, endpoint=True, dtype=np_t)
-        edges_d = torch.from_numpy(edges).to(dev)
-        counts = torch.empty(int(bins), dtype=torch.int64, device=dev)
-        N.check(lib.pvd_histogram(d.data_ptr(), dt, m.data_ptr(), mt, n, edges_d.data_ptr(), int(bins),
-                                  counts.data_ptr(), sh))
-        hist = counts.cpu().numpy()
-    cum_dvh = 1.0 - np.cumsum(hist) / int(st.count)
+        # statistics, numpy's edges and the counts on the device; one copy back
+        res = torch.empty(4 + bins, dtype=torch.int64, device=dev)
+        edges_d = torch.empty(bins + 1, dtype=d.dtype, device=dev)
+        N.check(lib.pvd_dvh(d.data_ptr(), dt, m.data_ptr(), mt, d.numel(), bins, edges_d.data_ptr(),
+                            res.data_ptr(), torch.cuda.current_stream(dev).cuda_stream))
+        host = res.cpu().numpy()
+    count, nonfinite = int(host[2]), int(host[3])
+    if count == 0:
+        raise ValueError("ROI mask is empty")
+    if nonfinite:
+        raise ValueError("autodetected range of [nan, nan] is not finite")
+    first, last = _key_values(host[:2].view(np.uint64), np_t)
+    if first == last:
+        first, last = first - 0.5, last + 0.5
+    edges = np.linspace(first, last, bins + 1, endpoint=True, dtype=np_t)
+    cum_dvh = 1.0 - np.cumsum(host[4:]) / count
     return edges[1:], cum_dvh
+
+
+def _key_values(keys: np.ndarray, np_t):
+    """Doses back from pvd_dvh's order-preserving keys (inverse of the device encoding)."""
+    if np_t is np.float32:
+        u = (keys & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+        b = np.where(u & np.uint32(0x80000000), u & np.uint32(0x7FFFFFFF), ~u).astype(np.uint32)
+        v = b.view(np.float32)
+    else:
+        sign = np.uint64(0x8000000000000000)
+        b = np.where(keys & sign, keys & np.uint64(0x7FFFFFFFFFFFFFFF), ~keys).astype(np.uint64)
+        v = b.view(np.float64)
+    return np_t(v[0]), np_t(v[1])
 
 
 # ---------------------------------------------------------------------------

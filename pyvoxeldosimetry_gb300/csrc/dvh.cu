@@ -82,6 +82,46 @@ __device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(
 __device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
+template <typename T> __device__ __forceinline__ T key_value(unsigned long long k);
+template <> __device__ __forceinline__ float key_value<float>(unsigned long long k) {
+  const unsigned int u = (unsigned int)k;
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+template <> __device__ __forceinline__ double key_value<double>(unsigned long long k) {
+  return __longlong_as_double((long long)((k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+// The bins+1 edges numpy's histogram uses, from the ROI statistics: range widened by
+// 0.5 on each side when empty, then np.linspace(first, last, bins + 1) in the dose's
+// type (numpy/_core/function_base.py `linspace`: step = (last - first) / bins,
+// edge i = i * step + first, the last edge = last; (i / bins) * (last - first) + first
+// when the step underflows to 0).  Nothing is written for an empty or non-finite ROI.
+template <typename T>
+__global__ void k_dvh_edges(const unsigned long long* __restrict__ acc, int bins, T* __restrict__ edges) {
+  if (acc[2] == 0ull || acc[3] != 0ull) return;
+  T first = key_value<T>(acc[0]), last = key_value<T>(acc[1]);
+  if (first == last) {
+    first = sub_rn(first, (T)0.5);
+    last = add_rn(last, (T)0.5);
+  }
+  const T delta = sub_rn(last, first);
+  const T div = (T)bins;
+  const T step = div_rn(delta, div);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= bins; i += gridDim.x * blockDim.x) {
+    T y;
+    if (i == bins)
+      y = last;
+    else if (step == (T)0)
+      y = add_rn(mul_rn(div_rn((T)i, div), delta), first);
+    else
+      y = add_rn(mul_rn((T)i, step), first);
+    edges[i] = y;
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ int bin_of(T x, T first, T denom, T nb, int bins, const T* __restrict__ edges) {
   const T f = mul_rn(div_rn(sub_rn(x, first), denom), nb);
@@ -92,10 +132,13 @@ __device__ __forceinline__ int bin_of(T x, T first, T denom, T nb, int bins, con
   return (int)i;
 }
 
+// acc (nullable): ROI statistics of k_roi_stats; nothing is counted for an empty or non-finite ROI
 template <typename T, typename M, bool SMEM>
 __global__ void __launch_bounds__(kDvhThreads) k_histogram(const T* __restrict__ dose, const M* __restrict__ mask,
                                                            long long n, const T* __restrict__ edges, int bins,
-                                                           unsigned long long* __restrict__ counts) {
+                                                           unsigned long long* __restrict__ counts,
+                                                           const unsigned long long* __restrict__ acc) {
+  if (acc && (acc[2] == 0ull || acc[3] != 0ull)) return;
   __shared__ unsigned int h[SMEM ? kSmemBins : 1];
   if (SMEM) {
     for (int b = threadIdx.x; b < bins; b += blockDim.x) h[b] = 0u;
@@ -132,13 +175,21 @@ static void launch_stats(const void* dose, const void* mask, long long n, unsign
 
 template <typename T, typename M>
 static void launch_hist(const void* dose, const void* mask, long long n, const void* edges, int bins,
-                        unsigned long long* counts, cudaStream_t st) {
+                        unsigned long long* counts, cudaStream_t st, const unsigned long long* acc = nullptr) {
   if (bins <= kSmemBins)
     k_histogram<T, M, true><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n,
-                                                                  (const T*)edges, bins, counts);
+                                                                  (const T*)edges, bins, counts, acc);
   else
     k_histogram<T, M, false><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n,
-                                                                   (const T*)edges, bins, counts);
+                                                                   (const T*)edges, bins, counts, acc);
+}
+
+template <typename T, typename M>
+static void launch_dvh(const void* dose, const void* mask, long long n, int bins, void* edges,
+                       unsigned long long* res, cudaStream_t st) {
+  k_roi_stats<T, M><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n, res);
+  k_dvh_edges<T><<<(bins + 256) / 256, 256, 0, st>>>(res, bins, (T*)edges);
+  launch_hist<T, M>(dose, mask, n, edges, bins, res + 4, st, res);
 }
 
 static double key_to_value(unsigned long long k, int dtype) {
@@ -222,6 +273,28 @@ extern "C" pvd_status pvd_histogram(const void* dose_d, int dose_dtype, const vo
   else
     (mask_dtype == PVD_DTYPE_U8) ? launch_hist<double, unsigned char>(dose_d, mask_d, n, edges_d, bins, c, st)
                                  : launch_hist<double, float>(dose_d, mask_d, n, edges_d, bins, c, st);
+  PVD_LAUNCH_CHECK("k_histogram");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_dvh(const void* dose_d, int dose_dtype, const void* mask_d, int mask_dtype, long long n,
+                              int bins, void* edges_d, long long* result_d, pvd_stream stream) {
+  if (!dose_d || !edges_d || !result_d) return set_error(PVD_ERR_ARG, "pvd_dvh: null argument");
+  if (n < 1 || bins < 1) return set_error(PVD_ERR_ARG, "pvd_dvh: need n >= 1 and bins >= 1");
+  if (!dtypes_ok(dose_dtype, mask_dtype))
+    return set_error(PVD_ERR_ARG, "pvd_dvh: dose must be PVD_DTYPE_F32/F64, mask PVD_DTYPE_U8/F32");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemsetAsync(result_d, 0xff, sizeof(long long), st);  // min key starts at all ones
+  if (e == cudaSuccess) e = cudaMemsetAsync(result_d + 1, 0, sizeof(long long) * (size_t)(3 + bins), st);
+  if (e != cudaSuccess) return set_error(PVD_ERR_CUDA, std::string("pvd_dvh: ") + cudaGetErrorString(e));
+  unsigned long long* res = (unsigned long long*)result_d;
+  if (dose_dtype == PVD_DTYPE_F32)
+    (mask_dtype == PVD_DTYPE_U8) ? launch_dvh<float, unsigned char>(dose_d, mask_d, n, bins, edges_d, res, st)
+                                 : launch_dvh<float, float>(dose_d, mask_d, n, bins, edges_d, res, st);
+  else
+    (mask_dtype == PVD_DTYPE_U8) ? launch_dvh<double, unsigned char>(dose_d, mask_d, n, bins, edges_d, res, st)
+                                 : launch_dvh<double, float>(dose_d, mask_d, n, bins, edges_d, res, st);
+  count_launch(2);
   PVD_LAUNCH_CHECK("k_histogram");
   return PVD_OK;
 }

@@ -75,3 +75,29 @@ def test_dvh_errors_match_the_reference():
     np.testing.assert_array_equal(c, c0)
     with pytest.raises(ValueError):
         calculate_dvh(d, m, 0)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_device_edges_equal_numpy_linspace(dtype):
+    """pvd_dvh computes numpy's histogram edges on the device; they must be np.linspace's."""
+    from pyvoxeldosimetry_gb300 import _native as N
+    lib = N.load()
+    rng = np.random.default_rng(12)
+    tiny = np.finfo(dtype).tiny
+    cases = [rng.gamma(2.0, 5.0, 5000).astype(dtype), np.full(100, dtype(3.25)),
+             (rng.random(777) * 3 * tiny).astype(dtype), (rng.standard_normal(999) * 1e6).astype(dtype)]
+    for dose in cases:
+        for bins in (1, 7, 1000):
+            d = torch.from_numpy(dose).cuda()
+            m = torch.ones(dose.shape, dtype=torch.uint8, device="cuda")
+            res = torch.empty(4 + bins, dtype=torch.int64, device="cuda")
+            edges = torch.empty(bins + 1, dtype=d.dtype, device="cuda")
+            dt = N.PVD_DTYPE_F32 if dtype is np.float32 else N.PVD_DTYPE_F64
+            N.check(lib.pvd_dvh(d.data_ptr(), dt, m.data_ptr(), N.PVD_DTYPE_U8, dose.size, bins, edges.data_ptr(),
+                                res.data_ptr(), torch.cuda.current_stream().cuda_stream))
+            first, last = dose.min(), dose.max()
+            if first == last:
+                first, last = first - 0.5, last + 0.5
+            np.testing.assert_array_equal(edges.cpu().numpy(), np.linspace(first, last, bins + 1, dtype=dtype))
+            h, _ = np.histogram(dose, bins=bins)
+            np.testing.assert_array_equal(res.cpu().numpy()[4:], h)

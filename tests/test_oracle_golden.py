@@ -129,3 +129,18 @@ def test_ac225_terms_are_reference(golden, tissue):
     ga = np.stack([ok.ac225_gamma(rg, e, i, tissue) for e, i in ok.AC_GAMMAS])
     np.testing.assert_allclose(al, golden[f"kgen_ac225_alpha_{tissue}"], rtol=1e-13, atol=0)
     np.testing.assert_allclose(ga, golden[f"kgen_ac225_gamma_{tissue}"], rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_restated_linspace_edges_equal_numpy(dtype):
+    """The GPU computes numpy's histogram edges with this restatement of linspace."""
+    from oracle import dvh as od
+    rng = np.random.default_rng(7)
+    tiny = np.finfo(dtype).tiny
+    cases = [(dtype(a), dtype(a + abs(b))) for a, b in rng.standard_normal((40, 2)) * 1e3]
+    cases += [(dtype(0.0), dtype(tiny * 3)), (dtype(-tiny), dtype(tiny)), (dtype(1.0), dtype(1.0 + np.finfo(dtype).eps))]
+    cases += [(dtype(x) - dtype(0.5), dtype(x) + dtype(0.5)) for x in (3.25, 1e7, -2.0)]
+    for first, last in cases:
+        for bins in (1, 3, 7, 1000, 20000):
+            np.testing.assert_array_equal(od.numpy_linspace_edges(first, last, bins),
+                                          np.linspace(first, last, bins + 1, endpoint=True, dtype=dtype))
