@@ -432,6 +432,13 @@ pvd_status pvd_resample(const float* src_d, int n0, int n1, int n2, float* out_d
                         const double* step, const double* origin, int order, float value_scale,
                         pvd_stream stream);
 
+/* pvd_resample as three one-axis passes (x, then y, then z; the spline is a tensor
+ * product): 4 (order 3) or 2 (order 1) taps per output and pass.  scratch_d: device
+ * float32 of at least n0*n1*m2 + n0*m1*m2 + 8*(m0+m1+m2) elements (scratch_elems). */
+pvd_status pvd_resample_separable(const float* src_d, int n0, int n1, int n2, float* out_d, int m0, int m1,
+                                  int m2, const double* step, const double* origin, int order, float value_scale,
+                                  float* scratch_d, long long scratch_elems, pvd_stream stream);
+
 /* ------------------------------------------------------------------------ */
 /* Dose-point kernels                                                         */
 /* ------------------------------------------------------------------------ */

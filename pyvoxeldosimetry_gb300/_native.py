@@ -43,7 +43,7 @@ EXPORTED_SYMBOLS = [
     "pvd_mc_plan_create", "pvd_mc_run", "pvd_mc_plan_destroy",
     "pvd_batch_execute", "pvd_batch_create", "pvd_batch_run", "pvd_batch_destroy",
     "pvd_roi_stats", "pvd_histogram", "pvd_dvh",
-    "pvd_bspline_prefilter", "pvd_resample",
+    "pvd_bspline_prefilter", "pvd_resample", "pvd_resample_separable",
     "pvd_radial_kernel",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
 ]
@@ -156,6 +156,8 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_bspline_prefilter": (st, [vp, vp, vp, i, i, i, vp]),
         "pvd_radial_kernel": (st, [C.POINTER(RadialTerm), i, d, i, i, i, C.POINTER(C.c_double), vp, vp]),
         "pvd_resample": (st, [vp, i, i, i, vp, i, i, i, C.POINTER(C.c_double), C.POINTER(C.c_double), i, f, vp]),
+        "pvd_resample_separable": (st, [vp, i, i, i, vp, i, i, i, C.POINTER(C.c_double), C.POINTER(C.c_double), i, f,
+                                        vp, C.c_longlong, vp]),
         "pvd_last_error": (st, [C.c_char_p, C.c_size_t]),
         "pvd_version": (i, []),
         "pvd_launch_count": (C.c_uint64, [i]),

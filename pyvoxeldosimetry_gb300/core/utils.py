@@ -357,8 +357,10 @@ def resample_volume(volume, input_spacing, output_spacing, order: int = 3, conse
             del scratch
             src = coef
         out = torch.empty(m, dtype=torch.float32, device=dev)
-        N.check(lib.pvd_resample(src.data_ptr(), *shape, out.data_ptr(), *m, (C.c_double * 3)(*step),
-                                 (C.c_double * 3)(*origin), order, scale, sh))
+        n_scr = shape[0] * shape[1] * m[2] + shape[0] * m[1] * m[2] + 8 * (m[0] + m[1] + m[2])
+        scratch = torch.empty(max(n_scr, 1), dtype=torch.float32, device=dev)
+        N.check(lib.pvd_resample_separable(src.data_ptr(), *shape, out.data_ptr(), *m, (C.c_double * 3)(*step),
+                                           (C.c_double * 3)(*origin), order, scale, scratch.data_ptr(), n_scr, sh))
         return _io.from_device(out, kind)
 
 
