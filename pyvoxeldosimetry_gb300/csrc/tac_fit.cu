@@ -18,6 +18,7 @@
 // HBM traffic per voxel: 4T bytes read, 8(n_par+1)+1 bytes written; the
 // kernel is FP64-throughput bound (exp and the normal equations per iteration).
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 
 #include "pvd_common.cuh"
@@ -515,94 +516,137 @@ __device__ void lm_par(const R* A, const R* g, const R* D, R delta, R& par, R* p
 }
 
 // Moré's Levenberg-Marquardt outer iteration (scaled trust region) with an
-// analytic Jacobian.  Returns MINPACK's info code: 1-4 success (ftol / xtol /
-// both / gtol), 5 evaluation budget exhausted, 6-8 tolerances too small, -1
-// non-finite cost.  `maxfev` counts model evaluations as a forward-difference
-// Jacobian would (N per Jacobian), so the budget matches curve_fit's.  fstop > 0
-// adds a success test (info 1): residual norm <= fstop.
+// analytic Jacobian, as a resumable state machine: lm_begin, then lm_tick until
+// it returns non-zero.  Each tick evaluates the normal equations when the last
+// step was accepted and makes one trial step, so a lane can interleave voxels at
+// tick granularity.  Info codes are MINPACK's: 1-4 success (ftol / xtol / both /
+// gtol), 5 evaluation budget exhausted, 6-8 tolerances too small, -1 non-finite
+// cost.  `maxfev` counts model evaluations as a forward-difference Jacobian
+// would (N per Jacobian), so the budget matches curve_fit's.  fstop > 0 adds a
+// success test (info 1): residual norm <= fstop.
+template <int M, typename R>
+struct LmState {
+  static constexpr int N = ModelTraits<M>::N;
+  R x[N], D[N], A[N * N], g[N];
+  R fnorm, delta, xnorm, par, gnorm, fstop;
+  int iter, nfev, maxfev;
+  bool need_jac;
+};
+
+template <int M, typename R>
+__device__ __forceinline__ int lm_begin(const FitArgs& a, const R* y, LmState<M, R>& s) {
+  s.nfev = 1;
+  s.fnorm = sqrt((R)2.0 * cost_at<M, R>(a, y, s.x));
+  if (!isfinite(s.fnorm)) return -1;
+  if (s.fnorm <= s.fstop) return 1;
+  s.delta = (R)0.0;
+  s.xnorm = (R)0.0;
+  s.par = (R)0.0;
+  s.gnorm = (R)0.0;
+  s.iter = 1;
+  s.need_jac = true;
+  return 0;
+}
+
+template <int M, typename R>
+__device__ __forceinline__ int lm_tick(const FitArgs& a, const R* y, LmState<M, R>& s) {
+  constexpr int N = ModelTraits<M>::N;
+  const R ftol = Lim<R>::tol(), xtol = Lim<R>::tol(), epsmch = Lim<R>::eps();
+  if (s.need_jac) {
+    normal_eq<M, R>(a, y, s.x, s.A, s.g);
+    s.nfev += N;
+    R acn[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) acn[j] = sqrt(s.A[j * N + j]);
+    if (s.iter == 1) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) s.D[j] = (acn[j] == (R)0.0) ? (R)1.0 : acn[j];
+      s.xnorm = dnorm<N, R>(s.D, s.x);
+      s.delta = (R)100.0 * s.xnorm;
+      if (s.delta == (R)0.0) s.delta = (R)100.0;
+    }
+    R gnorm = (R)0.0;
+    if (s.fnorm != (R)0.0) {
+#pragma unroll
+      for (int j = 0; j < N; ++j)
+        if (acn[j] != (R)0.0) gnorm = fmax(gnorm, fabs(s.g[j] / s.fnorm) / acn[j]);
+    }
+    s.gnorm = gnorm;
+    if (gnorm <= (R)0.0) return 4;  // gtol = 0
+#pragma unroll
+    for (int j = 0; j < N; ++j) s.D[j] = fmax(s.D[j], acn[j]);
+    s.need_jac = false;
+  }
+  // one trial step of the inner loop
+  R p[N], xt[N];
+  lm_par<N, R>(s.A, s.g, s.D, s.delta, s.par, p);
+#pragma unroll
+  for (int j = 0; j < N; ++j) xt[j] = s.x[j] + p[j];
+  const R pnorm = dnorm<N, R>(s.D, p);
+  if (s.iter == 1) s.delta = fmin(s.delta, pnorm);
+  const R fnorm1 = sqrt((R)2.0 * cost_at<M, R>(a, y, xt));
+  s.nfev += 1;
+  R actred = -(R)1.0;
+  if ((R)0.1 * fnorm1 < s.fnorm) actred = (R)1.0 - (fnorm1 / s.fnorm) * (fnorm1 / s.fnorm);
+  R jp2 = (R)0.0;  // ||J p||^2 = p^T A p
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    R row = (R)0.0;
+#pragma unroll
+    for (int c = 0; c < N; ++c) row += (c >= i ? s.A[i * N + c] : s.A[c * N + i]) * p[c];
+    jp2 += p[i] * row;
+  }
+  const R t1 = sqrt(fmax(jp2, (R)0.0)) / s.fnorm;
+  const R t2 = sqrt(s.par) * pnorm / s.fnorm;
+  const R prered = t1 * t1 + t2 * t2 / (R)0.5;
+  const R dirder = -(t1 * t1 + t2 * t2);
+  R ratio = (prered != (R)0.0) ? actred / prered : (R)0.0;
+  if (!isfinite(fnorm1)) ratio = (R)0.0;
+  if (ratio <= (R)0.25) {
+    R temp = (actred >= (R)0.0) ? (R)0.5 : (R)0.5 * dirder / (dirder + (R)0.5 * actred);
+    if ((R)0.1 * fnorm1 >= s.fnorm || temp < (R)0.1 || !isfinite(fnorm1)) temp = (R)0.1;
+    s.delta = temp * fmin(s.delta, pnorm / (R)0.1);
+    s.par = s.par / temp;
+  } else if (s.par == (R)0.0 || ratio >= (R)0.75) {
+    s.delta = pnorm / (R)0.5;
+    s.par = (R)0.5 * s.par;
+  }
+  const bool accepted = ratio >= (R)1e-4;
+  if (accepted) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) s.x[j] = xt[j];
+    s.fnorm = fnorm1;
+    s.xnorm = dnorm<N, R>(s.D, s.x);
+    if (s.fnorm <= s.fstop) return 1;  // the curve reproduces the samples to their own precision
+  }
+  int info = 0;
+  if (fabs(actred) <= ftol && prered <= ftol && (R)0.5 * ratio <= (R)1.0) info = 1;
+  if (s.delta <= xtol * s.xnorm) info = (info == 1) ? 3 : 2;
+  if (info) return info;
+  if (s.nfev >= s.maxfev) return 5;
+  if (fabs(actred) <= epsmch && prered <= epsmch && (R)0.5 * ratio <= (R)1.0) return 6;
+  if (s.delta <= epsmch * s.xnorm) return 7;
+  if (s.gnorm <= epsmch) return 8;
+  if (accepted) {  // next outer iteration
+    ++s.iter;
+    s.need_jac = true;
+  }
+  return 0;
+}
+
 template <int M, typename R>
 __device__ int lm_fit(const FitArgs& a, const R* y, R* x, int maxfev, R fstop = (R)0) {
   constexpr int N = ModelTraits<M>::N;
-  const R ftol = Lim<R>::tol(), xtol = Lim<R>::tol(), epsmch = Lim<R>::eps();
-  R A[N * N], g[N], D[N], p[N], xt[N];
-  int nfev = 1;
-  R fnorm = sqrt((R)2.0 * cost_at<M, R>(a, y, x));
-  if (!isfinite(fnorm)) return -1;
-  if (fnorm <= fstop) return 1;
-  R delta = (R)0.0, xnorm = (R)0.0, par = (R)0.0;
-  for (int iter = 1;; ++iter) {
-    normal_eq<M, R>(a, y, x, A, g);
-    nfev += N;
-    R acn[N];
+  LmState<M, R> s;
 #pragma unroll
-    for (int j = 0; j < N; ++j) acn[j] = sqrt(A[j * N + j]);
-    if (iter == 1) {
+  for (int j = 0; j < N; ++j) s.x[j] = x[j];
+  s.maxfev = maxfev;
+  s.fstop = fstop;
+  int info = lm_begin<M, R>(a, y, s);
+  while (info == 0) info = lm_tick<M, R>(a, y, s);
 #pragma unroll
-      for (int j = 0; j < N; ++j) D[j] = (acn[j] == (R)0.0) ? (R)1.0 : acn[j];
-      xnorm = dnorm<N, R>(D, x);
-      delta = (R)100.0 * xnorm;
-      if (delta == (R)0.0) delta = (R)100.0;
-    }
-    R gnorm = (R)0.0;
-    if (fnorm != (R)0.0) {
-#pragma unroll
-      for (int j = 0; j < N; ++j)
-        if (acn[j] != (R)0.0) gnorm = fmax(gnorm, fabs(g[j] / fnorm) / acn[j]);
-    }
-    if (gnorm <= (R)0.0) return 4;  // gtol = 0
-#pragma unroll
-    for (int j = 0; j < N; ++j) D[j] = fmax(D[j], acn[j]);
-    R ratio = (R)0.0;
-    do {
-      lm_par<N, R>(A, g, D, delta, par, p);
-#pragma unroll
-      for (int j = 0; j < N; ++j) xt[j] = x[j] + p[j];
-      const R pnorm = dnorm<N, R>(D, p);
-      if (iter == 1) delta = fmin(delta, pnorm);
-      const R fnorm1 = sqrt((R)2.0 * cost_at<M, R>(a, y, xt));
-      nfev += 1;
-      R actred = -(R)1.0;
-      if ((R)0.1 * fnorm1 < fnorm) actred = (R)1.0 - (fnorm1 / fnorm) * (fnorm1 / fnorm);
-      R jp2 = (R)0.0;  // ||J p||^2 = p^T A p
-#pragma unroll
-      for (int i = 0; i < N; ++i) {
-        R row = (R)0.0;
-#pragma unroll
-        for (int c = 0; c < N; ++c) row += (c >= i ? A[i * N + c] : A[c * N + i]) * p[c];
-        jp2 += p[i] * row;
-      }
-      const R t1 = sqrt(fmax(jp2, (R)0.0)) / fnorm;
-      const R t2 = sqrt(par) * pnorm / fnorm;
-      const R prered = t1 * t1 + t2 * t2 / (R)0.5;
-      const R dirder = -(t1 * t1 + t2 * t2);
-      ratio = (prered != (R)0.0) ? actred / prered : (R)0.0;
-      if (!isfinite(fnorm1)) ratio = (R)0.0;
-      if (ratio <= (R)0.25) {
-        R temp = (actred >= (R)0.0) ? (R)0.5 : (R)0.5 * dirder / (dirder + (R)0.5 * actred);
-        if ((R)0.1 * fnorm1 >= fnorm || temp < (R)0.1 || !isfinite(fnorm1)) temp = (R)0.1;
-        delta = temp * fmin(delta, pnorm / (R)0.1);
-        par = par / temp;
-      } else if (par == (R)0.0 || ratio >= (R)0.75) {
-        delta = pnorm / (R)0.5;
-        par = (R)0.5 * par;
-      }
-      if (ratio >= (R)1e-4) {
-#pragma unroll
-        for (int j = 0; j < N; ++j) x[j] = xt[j];
-        fnorm = fnorm1;
-        xnorm = dnorm<N, R>(D, x);
-        if (fnorm <= fstop) return 1;  // the curve reproduces the samples to their own precision
-      }
-      int info = 0;
-      if (fabs(actred) <= ftol && prered <= ftol && (R)0.5 * ratio <= (R)1.0) info = 1;
-      if (delta <= xtol * xnorm) info = (info == 1) ? 3 : 2;
-      if (info) return info;
-      if (nfev >= maxfev) return 5;
-      if (fabs(actred) <= epsmch && prered <= epsmch && (R)0.5 * ratio <= (R)1.0) return 6;
-      if (delta <= epsmch * xnorm) return 7;
-      if (gnorm <= epsmch) return 8;
-    } while (ratio < (R)1e-4);
-  }
+  for (int j = 0; j < N; ++j) x[j] = s.x[j];
+  return info;
 }
 
 // Fallbacks of a failed fit, the AUC and the stores of one voxel.  good: the
@@ -741,20 +785,20 @@ __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long n
 }
 
 
-// Variable-projection fit of f4a (PVD_FIT_VARPRO), one thread per voxel with
-// load balancing inside each block.  Phase 1 (every voxel): exponential-peeling
-// start, the FP32 iteration (PVD_FIT_MIXED) and at most kShortFev FP64
-// evaluations.  Most voxels converge there.  The rest (nearly equal rates: the
-// projected cost has a long curved valley that the trust region crosses in
-// many small steps) go to a queue in shared memory with their current rates;
-// each time 128 are queued the whole block continues them in FP64 with the
-// full budget, so the long iterations run in full warps instead of holding a
-// warp of finished voxels each.  FP64 iterations also stop once the curve
-// reproduces the float32 samples to their rounding (2^-24 relative each).
+// Variable-projection fit of f4a (PVD_FIT_VARPRO) with lane refill.  The number
+// of trust-region steps differs widely between voxels (nearly equal rates make a
+// long curved valley), so one voxel per thread leaves most lanes of a warp idle.
+// Here every block owns a contiguous range of voxels and each lane steps its
+// voxel one tick at a time (lm_tick); when a lane's voxel is done the warp takes
+// the next voxels of the range from a shared-memory counter (one atomic per warp,
+// lane offsets from the ballot), so lanes stay busy until the range is exhausted.
+// FP32 and FP64 run as two launches (PVD_FIT_MIXED): the first from the
+// exponential-peeling start, handing its rates to the second through params;
+// a warp never mixes the two precisions.  FP64 iterations also stop once the
+// curve reproduces the float32 samples to their rounding (2^-24 relative each).
 // The amplitudes are then solved at the converged rates in FP64; the fast
 // component is stored first.
 constexpr int kVpThreads = 128;
-constexpr int kShortFev = 30;  // FP64 evaluations in phase 1
 
 template <int TM>
 struct VpVoxel {
@@ -790,6 +834,25 @@ __device__ __forceinline__ void vp_load(const FitArgs& a, const float* __restric
   d.fstop = 2.0 * 5.9604644775390625e-8 * sqrt(yn);
 }
 
+// the starting rates: exponential peeling, or p0
+template <int TM>
+__device__ __forceinline__ void vp_start(const FitArgs& a, const VpVoxel<TM>& d, double* lam) {
+  double p[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) p[i] = a.p0[i];
+  if (a.p0_peel && d.finite) {
+    double yA = 0.0, yB = 0.0;
+#pragma unroll
+    for (int k = 0; k < TM; ++k) {
+      if (k == a.T - 2) yA = d.y[k];
+      if (k == a.T - 1) yB = d.y[k];
+    }
+    peel_biexp4(a, d.y[0], d.y[1], yA, yB, a.t[a.T - 2], a.t[a.T - 1], p);
+  }
+  lam[0] = p[1];
+  lam[1] = p[3];
+}
+
 // amplitudes at the final rates, fallbacks, AUC and stores
 template <int TM>
 __device__ __forceinline__ void vp_store(const FitArgs& a, const VpVoxel<TM>& d, const double* lam, bool good,
@@ -812,81 +875,80 @@ __device__ __forceinline__ void vp_store(const FitArgs& a, const VpVoxel<TM>& d,
   store_fit<M_F4A>(a, p, good, ymax, v, nvox, params, auc, ok, auc32);
 }
 
-template <int MV>
+// STAGE 0: FP32 from the peeling start, rates handed over in params[1], params[3].
+// STAGE 1: FP64 from those rates (PVD_FIT_MIXED) or from the start, then the stores.
+template <int MV, int STAGE>
 __global__ void __launch_bounds__(kVpThreads) k_tac_fit_vp(FitArgs a, const float* __restrict__ acts, long long nvox,
-                                                           double* __restrict__ params, double* __restrict__ auc,
-                                                           unsigned char* __restrict__ ok, float* __restrict__ auc32) {
+                                                           long long per_block, double* __restrict__ params,
+                                                           double* __restrict__ auc, unsigned char* __restrict__ ok,
+                                                           float* __restrict__ auc32) {
   constexpr int TM = ModelTraits<MV>::TMAX;
-  __shared__ long long q_vox[2 * kVpThreads];
-  __shared__ double q_lam[2 * kVpThreads][2];
-  __shared__ int q_n;
-  const int tid = threadIdx.x;
-  if (tid == 0) q_n = 0;
+  using R = typename std::conditional<STAGE == 0, float, double>::type;
+  __shared__ unsigned long long next;
+  const long long r0 = (long long)blockIdx.x * per_block;
+  const long long r1 = min(nvox, r0 + per_block);
+  if (threadIdx.x == 0) next = (unsigned long long)r0;
   __syncthreads();
-  for (long long base = (long long)blockIdx.x * kVpThreads; base < nvox; base += (long long)gridDim.x * kVpThreads) {
-    const long long v = base + tid;
-    if (v < nvox) {  // phase 1
-      VpVoxel<TM> d;
-      vp_load<TM>(a, acts, nvox, v, d);
-      double p[4];
-#pragma unroll
-      for (int i = 0; i < 4; ++i) p[i] = a.p0[i];
-      if (a.p0_peel && d.finite) {
-        double yA = 0.0, yB = 0.0;
-#pragma unroll
-        for (int k = 0; k < TM; ++k) {
-          if (k == a.T - 2) yA = d.y[k];
-          if (k == a.T - 1) yB = d.y[k];
-        }
-        peel_biexp4(a, d.y[0], d.y[1], yA, yB, a.t[a.T - 2], a.t[a.T - 1], p);
-      }
-      double lam[2] = {p[1], p[3]};
-      int info = -1;
-      if (d.finite && a.T >= 4) {
-        if (a.mixed) {
-          float ywf[TM], lf[2] = {(float)lam[0], (float)lam[1]};
-#pragma unroll
-          for (int k = 0; k < TM; ++k) ywf[k] = (float)d.yw[k];
-          lm_fit<MV, float>(a, ywf, lf, a.max_fev);
-          if (isfinite(lf[0]) && isfinite(lf[1])) {
-            lam[0] = lf[0];
-            lam[1] = lf[1];
+  const int lane = threadIdx.x & 31;
+  VpVoxel<TM> d;
+  LmState<MV, R> s;
+  R yr[TM];
+  double lam0[2] = {0.0, 0.0};  // start of the stage (STAGE 0 keeps it for a non-finite FP32 result)
+  long long v = 0;
+  bool alive = false, exhausted = r0 >= r1;
+  while (true) {
+    int fin = 0;  // non-zero: this lane's voxel is done, with this info code
+    const unsigned need = __ballot_sync(0xffffffffu, !alive && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(&next, (unsigned long long)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if ((need >> lane) & 1u) {
+        const long long mine = (long long)base + __popc(need & ((1u << lane) - 1u));
+        if (mine < r1) {
+          v = mine;
+          vp_load<TM>(a, acts, nvox, v, d);
+          if (STAGE == 1 && a.mixed) {
+            lam0[0] = params[1 * nvox + v];
+            lam0[1] = params[3 * nvox + v];
+          } else {
+            vp_start<TM>(a, d, lam0);
           }
+#pragma unroll
+          for (int k = 0; k < TM; ++k) yr[k] = (R)d.yw[k];
+          s.x[0] = (R)lam0[0];
+          s.x[1] = (R)lam0[1];
+          s.maxfev = a.max_fev;
+          s.fstop = STAGE == 0 ? (R)0 : (R)d.fstop;
+          int info = -1;
+          if (d.finite && a.T >= 4 && isfinite(lam0[0]) && isfinite(lam0[1])) info = lm_begin<MV, R>(a, yr, s);
+          if (info == 0)
+            alive = true;
+          else
+            fin = info;  // settled at the start
         }
-        info = lm_fit<MV, double>(a, d.yw, lam, min(a.max_fev, kShortFev), d.fstop);
       }
-      if (info == 5 && a.max_fev > kShortFev && isfinite(lam[0]) && isfinite(lam[1])) {
-        const int pos = atomicAdd(&q_n, 1);  // < 2 * kVpThreads: drained below whenever it reaches kVpThreads
-        q_vox[pos] = v;
-        q_lam[pos][0] = lam[0];
-        q_lam[pos][1] = lam[1];
+      if ((long long)base + __popc(need) >= r1) exhausted = true;  // the same for every lane
+    }
+    if (alive) {
+      const int info = lm_tick<MV, R>(a, yr, s);
+      if (info != 0) {
+        alive = false;
+        fin = info;
+      }
+    }
+    if (fin != 0) {
+      if (STAGE == 0) {
+        const bool f = isfinite(s.x[0]) && isfinite(s.x[1]);
+        params[1 * nvox + v] = f ? (double)s.x[0] : lam0[0];
+        params[3 * nvox + v] = f ? (double)s.x[1] : lam0[1];
       } else {
-        vp_store<TM>(a, d, lam, info >= 1 && info <= 4, v, nvox, params, auc, ok, auc32);
+        double lam[2] = {(double)s.x[0], (double)s.x[1]};
+        vp_store<TM>(a, d, lam, fin >= 1 && fin <= 4, v, nvox, params, auc, ok, auc32);
       }
     }
-    __syncthreads();
-    const int n = q_n;
-    if (n >= kVpThreads) {  // phase 2 on a full block of queued voxels
-      const int pos = n - kVpThreads + tid;
-      const long long vq = q_vox[pos];
-      double lam[2] = {q_lam[pos][0], q_lam[pos][1]};
-      __syncthreads();
-      if (tid == 0) q_n = n - kVpThreads;
-      VpVoxel<TM> d;
-      vp_load<TM>(a, acts, nvox, vq, d);
-      const int info = lm_fit<MV, double>(a, d.yw, lam, a.max_fev - kShortFev, d.fstop);
-      vp_store<TM>(a, d, lam, info >= 1 && info <= 4, vq, nvox, params, auc, ok, auc32);
-    }
-    __syncthreads();
-  }
-  const int n = q_n;  // the rest of the queue
-  if (tid < n) {
-    const long long vq = q_vox[tid];
-    double lam[2] = {q_lam[tid][0], q_lam[tid][1]};
-    VpVoxel<TM> d;
-    vp_load<TM>(a, acts, nvox, vq, d);
-    const int info = lm_fit<MV, double>(a, d.yw, lam, a.max_fev - kShortFev, d.fstop);
-    vp_store<TM>(a, d, lam, info >= 1 && info <= 4, vq, nvox, params, auc, ok, auc32);
+    if (exhausted && !__any_sync(0xffffffffu, alive)) break;
   }
 }
 
@@ -931,16 +993,30 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
   const int threads = 128;
   const int blocks = (int)std::min<long long>((n_vox + threads - 1) / threads, 152LL * 64);
   if (flags & PVD_FIT_VARPRO) {
-    const int vblocks = (int)std::min<long long>((n_vox + kVpThreads - 1) / kVpThreads, 152LL * 16);
+    // blocks own contiguous voxel ranges; a few blocks per SM keep the refill local
+    const long long nblk = std::min<long long>((n_vox + kVpThreads - 1) / kVpThreads, 152LL * 8);
+    const long long per_block = (n_vox + nblk - 1) / nblk;
+    const int g = (int)((n_vox + per_block - 1) / per_block);
+#define PVD_VP_LAUNCH(MV)                                                                                   \
+  {                                                                                                         \
+    if (a.mixed) {                                                                                          \
+      k_tac_fit_vp<MV, 0><<<g, kVpThreads, 0, st>>>(a, acts_d, n_vox, per_block, params_d, auc_d, ok_d,     \
+                                                    auc_f32_d);                                             \
+      PVD_LAUNCH_CHECK("k_tac_fit_vp<fp32>");                                                               \
+    }                                                                                                       \
+    k_tac_fit_vp<MV, 1><<<g, kVpThreads, 0, st>>>(a, acts_d, n_vox, per_block, params_d, auc_d, ok_d,       \
+                                                  auc_f32_d);                                               \
+    PVD_LAUNCH_CHECK("k_tac_fit_vp<fp64>");                                                                 \
+  }
     if (n_times == 4)
-      k_tac_fit_vp<M_F4A_VP4><<<vblocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
+      PVD_VP_LAUNCH(M_F4A_VP4)
     else if (n_times <= 6)
-      k_tac_fit_vp<M_F4A_VP6><<<vblocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
+      PVD_VP_LAUNCH(M_F4A_VP6)
     else if (n_times <= 8)
-      k_tac_fit_vp<M_F4A_VP8><<<vblocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
+      PVD_VP_LAUNCH(M_F4A_VP8)
     else
-      k_tac_fit_vp<M_F4A_VP16><<<vblocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);
-    PVD_LAUNCH_CHECK("k_tac_fit_vp");
+      PVD_VP_LAUNCH(M_F4A_VP16)
+#undef PVD_VP_LAUNCH
     return PVD_OK;
   }
   switch (model) {
