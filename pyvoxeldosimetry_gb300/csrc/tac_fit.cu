@@ -36,6 +36,9 @@ enum Model {
 struct FitArgs {
   double t[PVD_MAX_TIMEPOINTS];
   double w[PVD_MAX_TIMEPOINTS];  // residual multipliers (1 / sigma)
+  float tf[PVD_MAX_TIMEPOINTS];  // float copies for the FP32 iterations (a conversion from
+  float wf[PVD_MAX_TIMEPOINTS];  // double per use would run on GB300's slow FP64 pipe)
+  float lam_phys_f;
   double p0[5];
   int T;
   double lam_phys;               // ln2 / physical half-life (models with lambda_phys)
@@ -48,6 +51,17 @@ struct FitArgs {
   double f32_scale;              // scale of the optional float32 copy of the AUC
   int mixed;                     // FP32 Levenberg-Marquardt, then FP64 from its end point
 };
+
+// sample time, residual weight and physical decay constant in the iteration's precision
+template <typename R> __device__ __forceinline__ R t_at(const FitArgs& a, int k);
+template <> __device__ __forceinline__ double t_at<double>(const FitArgs& a, int k) { return a.t[k]; }
+template <> __device__ __forceinline__ float t_at<float>(const FitArgs& a, int k) { return a.tf[k]; }
+template <typename R> __device__ __forceinline__ R w_at(const FitArgs& a, int k);
+template <> __device__ __forceinline__ double w_at<double>(const FitArgs& a, int k) { return a.w[k]; }
+template <> __device__ __forceinline__ float w_at<float>(const FitArgs& a, int k) { return a.wf[k]; }
+template <typename R> __device__ __forceinline__ R lp_of(const FitArgs& a);
+template <> __device__ __forceinline__ double lp_of<double>(const FitArgs& a) { return a.lam_phys; }
+template <> __device__ __forceinline__ float lp_of<float>(const FitArgs& a) { return a.lam_phys_f; }
 
 // Start for the two-exponential model f4a from "exponential peeling": the slow
 // rate from the last two samples (yA at tA, yB at tB), the fast one from what it
@@ -243,12 +257,12 @@ struct VpBasis {
 
 template <int TM, typename R>
 __device__ __forceinline__ R vp_project(const FitArgs& a, const R* y, const R* p, VpBasis<TM, R>& b) {
-  const R lp = (R)a.lam_phys;
+  const R lp = lp_of<R>(a);
   R n1 = (R)0;
 #pragma unroll
   for (int j = 0; j < TM; ++j) {
     if (j < a.T) {
-      const R w = (R)a.w[j], t = (R)a.t[j];
+      const R w = w_at<R>(a, j), t = t_at<R>(a, j);
       b.e1[j] = w * exp(-(p[0] + lp) * t);
       b.e2[j] = w * exp(-(p[1] + lp) * t);
     } else {
@@ -318,7 +332,7 @@ __device__ __forceinline__ R vp_normal_eq(const FitArgs& a, const R* y, const R*
   R u1 = (R)0, u2 = (R)0, v1 = (R)0, v2 = (R)0;
 #pragma unroll
   for (int j = 0; j < TM; ++j) {
-    const R t = j < a.T ? (R)a.t[j] : (R)0;
+    const R t = j < a.T ? t_at<R>(a, j) : (R)0;
     const R we1 = b.r11 * b.e1[j], we2 = b.r12 * b.e1[j] + b.r22 * b.e2[j];
     j1[j] = -t * we1 * b.c1;
     j2[j] = -t * we2 * b.c2;
@@ -366,8 +380,8 @@ __device__ R normal_eq(const FitArgs& a, const R* y, const R* p, R* A, R* g) {
   R cost = (R)0;
   for (int k = 0; k < a.T; ++k) {
     R j[N];
-    const R w = (R)a.w[k];
-    const R f = ModelTraits<M>::template eval<R>(p, (R)a.t[k], (R)a.lam_phys, j);
+    const R w = w_at<R>(a, k);
+    const R f = ModelTraits<M>::template eval<R>(p, t_at<R>(a, k), lp_of<R>(a), j);
     const R r = w * (f - y[k]);
 #pragma unroll
     for (int i = 0; i < N; ++i) j[i] *= w;
@@ -393,7 +407,7 @@ __device__ R cost_at(const FitArgs& a, const R* y, const R* p) {
   R cost = (R)0;
   for (int k = 0; k < a.T; ++k) {
     R j[N];
-    const R r = (R)a.w[k] * (ModelTraits<M>::template eval<R>(p, (R)a.t[k], (R)a.lam_phys, j) - y[k]);
+    const R r = w_at<R>(a, k) * (ModelTraits<M>::template eval<R>(p, t_at<R>(a, k), lp_of<R>(a), j) - y[k]);
     cost += r * r;
   }
   return (R)0.5 * cost;
@@ -972,7 +986,10 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
   for (int k = 0; k < n_times; ++k) {
     a.t[k] = times[k];
     a.w[k] = weights ? weights[k] : 1.0;
+    a.tf[k] = (float)a.t[k];
+    a.wf[k] = (float)a.w[k];
   }
+  a.lam_phys_f = (float)lam_phys;
   for (int i = 0; i < 5; ++i) a.p0[i] = p0 ? p0[i] : 0.0;
   a.lam_phys = lam_phys;
   a.auc_limit = auc_limit;
