@@ -799,6 +799,104 @@ __global__ void k_tac_fit(FitArgs a, const float* __restrict__ acts, long long n
 }
 
 
+// Lane refill over a block's voxel range [r0, r1): each lane steps its voxel with
+// tick(); when it is done (non-zero info) finish(info) stores it and the warp takes
+// the next voxels from the shared-memory counter `next` (one atomic per warp, lane
+// offsets from the ballot).  init(v) loads voxel v and returns 0 to start iterating
+// or the final info of a voxel settled at once.  Every lane of the warp runs the
+// loop; it ends when the range is exhausted and no lane is still iterating, and
+// every voxel's iteration is bounded by its evaluation budget.
+template <class Init, class Tick, class Finish>
+__device__ __forceinline__ void refill_loop(long long r0, long long r1, unsigned long long* next, Init init,
+                                            Tick tick, Finish finish) {
+  const int lane = threadIdx.x & 31;
+  bool alive = false, exhausted = r0 >= r1;
+  while (true) {
+    int fin = 0;
+    const unsigned need = __ballot_sync(0xffffffffu, !alive && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(next, (unsigned long long)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if ((need >> lane) & 1u) {
+        const long long mine = (long long)base + __popc(need & ((1u << lane) - 1u));
+        if (mine < r1) {
+          const int info = init(mine);
+          if (info == 0)
+            alive = true;
+          else
+            fin = info;  // settled at the start
+        }
+      }
+      if ((long long)base + __popc(need) >= r1) exhausted = true;  // the same for every lane
+    }
+    if (alive) {
+      const int info = tick();
+      if (info != 0) {
+        alive = false;
+        fin = info;
+      }
+    }
+    if (fin != 0) finish(fin);
+    if (exhausted && !__any_sync(0xffffffffu, alive)) break;
+  }
+}
+
+// Other models, FP64 (the reference-parity path): one lane per voxel at a time with refill.
+template <int M>
+__global__ void __launch_bounds__(128) k_tac_fit_sched(FitArgs a, const float* __restrict__ acts, long long nvox,
+                                                       long long per_block, double* __restrict__ params,
+                                                       double* __restrict__ auc, unsigned char* __restrict__ ok,
+                                                       float* __restrict__ auc32) {
+  constexpr int N = ModelTraits<M>::N;
+  __shared__ unsigned long long next;
+  const long long r0 = (long long)blockIdx.x * per_block;
+  const long long r1 = min(nvox, r0 + per_block);
+  if (threadIdx.x == 0) next = (unsigned long long)r0;
+  __syncthreads();
+  double y[PVD_MAX_TIMEPOINTS];
+  double ymax = 0.0;
+  LmState<M, double> s;
+  long long v = 0;
+  auto init = [&](long long vv) -> int {
+    v = vv;
+    bool finite = true;
+    ymax = 0.0;
+    for (int k = 0; k < a.T; ++k) {
+      y[k] = (double)__ldg(acts + (long long)k * nvox + v);
+      finite = finite && isfinite(y[k]);
+    }
+    if (a.force_zero_at_t0) {
+      const double y0 = y[0];
+      for (int k = 0; k < a.T; ++k) y[k] -= y0;
+      y[0] = 0.0;
+    }
+    for (int k = 0; k < a.T; ++k) ymax = fmax(ymax, fabs(y[k]));
+#pragma unroll
+    for (int i = 0; i < N; ++i) s.x[i] = a.p0[i];
+    if (M == M_MONO_LAMBDA && a.p0_from_data) {
+      s.x[0] = y[0];
+      s.x[1] = a.lam_phys;
+    }
+    if constexpr (M == M_F4A) {
+      if (a.p0_peel && finite && a.T >= 4) peel_biexp(a, y, s.x);
+    }
+    s.maxfev = a.max_fev;
+    s.fstop = 0.0;
+    if (!(finite && a.T >= N)) return -1;
+    return lm_begin<M, double>(a, y, s);
+  };
+  auto tick = [&]() -> int { return lm_tick<M, double>(a, y, s); };
+  auto finish = [&](int info) {
+    double p[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) p[i] = s.x[i];
+    store_fit<M>(a, p, info >= 1 && info <= 4, ymax, v, nvox, params, auc, ok, auc32);
+  };
+  refill_loop(r0, r1, &next, init, tick, finish);
+}
+
 // Variable-projection fit of f4a (PVD_FIT_VARPRO) with lane refill.  The number
 // of trust-region steps differs widely between voxels (nearly equal rates make a
 // long curved valley), so one voxel per thread leaves most lanes of a warp idle.
@@ -903,67 +1001,41 @@ __global__ void __launch_bounds__(kVpThreads) k_tac_fit_vp(FitArgs a, const floa
   const long long r1 = min(nvox, r0 + per_block);
   if (threadIdx.x == 0) next = (unsigned long long)r0;
   __syncthreads();
-  const int lane = threadIdx.x & 31;
   VpVoxel<TM> d;
   LmState<MV, R> s;
   R yr[TM];
   double lam0[2] = {0.0, 0.0};  // start of the stage (STAGE 0 keeps it for a non-finite FP32 result)
   long long v = 0;
-  bool alive = false, exhausted = r0 >= r1;
-  while (true) {
-    int fin = 0;  // non-zero: this lane's voxel is done, with this info code
-    const unsigned need = __ballot_sync(0xffffffffu, !alive && !exhausted);
-    if (need) {
-      const int leader = __ffs(need) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(&next, (unsigned long long)__popc(need));
-      base = __shfl_sync(0xffffffffu, base, leader);
-      if ((need >> lane) & 1u) {
-        const long long mine = (long long)base + __popc(need & ((1u << lane) - 1u));
-        if (mine < r1) {
-          v = mine;
-          vp_load<TM>(a, acts, nvox, v, d);
-          if (STAGE == 1 && a.mixed) {
-            lam0[0] = params[1 * nvox + v];
-            lam0[1] = params[3 * nvox + v];
-          } else {
-            vp_start<TM>(a, d, lam0);
-          }
+  auto init = [&](long long vv) -> int {
+    v = vv;
+    vp_load<TM>(a, acts, nvox, v, d);
+    if (STAGE == 1 && a.mixed) {
+      lam0[0] = params[1 * nvox + v];
+      lam0[1] = params[3 * nvox + v];
+    } else {
+      vp_start<TM>(a, d, lam0);
+    }
 #pragma unroll
-          for (int k = 0; k < TM; ++k) yr[k] = (R)d.yw[k];
-          s.x[0] = (R)lam0[0];
-          s.x[1] = (R)lam0[1];
-          s.maxfev = a.max_fev;
-          s.fstop = STAGE == 0 ? (R)0 : (R)d.fstop;
-          int info = -1;
-          if (d.finite && a.T >= 4 && isfinite(lam0[0]) && isfinite(lam0[1])) info = lm_begin<MV, R>(a, yr, s);
-          if (info == 0)
-            alive = true;
-          else
-            fin = info;  // settled at the start
-        }
-      }
-      if ((long long)base + __popc(need) >= r1) exhausted = true;  // the same for every lane
+    for (int k = 0; k < TM; ++k) yr[k] = (R)d.yw[k];
+    s.x[0] = (R)lam0[0];
+    s.x[1] = (R)lam0[1];
+    s.maxfev = a.max_fev;
+    s.fstop = STAGE == 0 ? (R)0 : (R)d.fstop;
+    if (!(d.finite && a.T >= 4 && isfinite(lam0[0]) && isfinite(lam0[1]))) return -1;
+    return lm_begin<MV, R>(a, yr, s);
+  };
+  auto tick = [&]() -> int { return lm_tick<MV, R>(a, yr, s); };
+  auto finish = [&](int info) {
+    if (STAGE == 0) {
+      const bool f = isfinite(s.x[0]) && isfinite(s.x[1]);
+      params[1 * nvox + v] = f ? (double)s.x[0] : lam0[0];
+      params[3 * nvox + v] = f ? (double)s.x[1] : lam0[1];
+    } else {
+      double lam[2] = {(double)s.x[0], (double)s.x[1]};
+      vp_store<TM>(a, d, lam, info >= 1 && info <= 4, v, nvox, params, auc, ok, auc32);
     }
-    if (alive) {
-      const int info = lm_tick<MV, R>(a, yr, s);
-      if (info != 0) {
-        alive = false;
-        fin = info;
-      }
-    }
-    if (fin != 0) {
-      if (STAGE == 0) {
-        const bool f = isfinite(s.x[0]) && isfinite(s.x[1]);
-        params[1 * nvox + v] = f ? (double)s.x[0] : lam0[0];
-        params[3 * nvox + v] = f ? (double)s.x[1] : lam0[1];
-      } else {
-        double lam[2] = {(double)s.x[0], (double)s.x[1]};
-        vp_store<TM>(a, d, lam, fin >= 1 && fin <= 4, v, nvox, params, auc, ok, auc32);
-      }
-    }
-    if (exhausted && !__any_sync(0xffffffffu, alive)) break;
-  }
+  };
+  refill_loop(r0, r1, &next, init, tick, finish);
 }
 
 }  // namespace pvd
@@ -1036,10 +1108,16 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
 #undef PVD_VP_LAUNCH
     return PVD_OK;
   }
+  const long long sblk = std::min<long long>((n_vox + 127) / 128, 152LL * 8);
+  const long long s_per = (n_vox + sblk - 1) / sblk;
+  const int sgrid = (int)((n_vox + s_per - 1) / s_per);
   switch (model) {
-#define PVD_FIT_CASE(M)                                                                    \
-  case M:                                                                                  \
-    k_tac_fit<M><<<blocks, threads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d); \
+#define PVD_FIT_CASE(M)                                                                                \
+  case M:                                                                                              \
+    if (a.mixed)                                                                                       \
+      k_tac_fit<M><<<blocks, threads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d);    \
+    else                                                                                               \
+      k_tac_fit_sched<M><<<sgrid, 128, 0, st>>>(a, acts_d, n_vox, s_per, params_d, auc_d, ok_d, auc_f32_d); \
     break;
     PVD_FIT_CASE(M_MONO_LAMBDA)
     PVD_FIT_CASE(M_F2)
