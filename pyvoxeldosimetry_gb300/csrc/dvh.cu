@@ -17,6 +17,7 @@
 // Counts are accumulated per block in shared memory (bins <= kSmemBins), then
 // added to 64-bit global counters.
 #include <algorithm>
+#include <cstdint>
 #include <cstring>
 
 #include "pvd_common.cuh"
@@ -40,24 +41,68 @@ __device__ __forceinline__ bool in_roi(const M* mask, long long i) {
   return mask == nullptr || __ldg(mask + i) > (M)0;
 }
 
+// Four consecutive voxels per load: float4 / two double2 for the dose, uchar4 / float4
+// for the mask (VEC: the pointers are 16-byte aligned), else four scalar loads.
+// Dose and mask are loaded together, so each thread keeps both in flight.
+template <typename T, bool VEC>
+__device__ __forceinline__ void load4(const T* __restrict__ p, long long i, T* x) {
+  if constexpr (VEC && sizeof(T) == 4) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p + i));
+    x[0] = v.x, x[1] = v.y, x[2] = v.z, x[3] = v.w;
+  } else if constexpr (VEC) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p + i));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(p + i + 2));
+    x[0] = a.x, x[1] = a.y, x[2] = b.x, x[3] = b.y;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) x[k] = __ldg(p + i + k);
+  }
+}
+template <typename M, bool VEC>
+__device__ __forceinline__ void roi4(const M* __restrict__ m, long long i, bool* in) {
+  if (m == nullptr) {
+    in[0] = in[1] = in[2] = in[3] = true;
+  } else if constexpr (VEC && sizeof(M) == 1) {
+    const uchar4 v = __ldg(reinterpret_cast<const uchar4*>(m + i));
+    in[0] = v.x > 0, in[1] = v.y > 0, in[2] = v.z > 0, in[3] = v.w > 0;
+  } else if constexpr (VEC) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(m + i));
+    in[0] = v.x > 0.f, in[1] = v.y > 0.f, in[2] = v.z > 0.f, in[3] = v.w > 0.f;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) in[k] = __ldg(m + i + k) > (M)0;
+  }
+}
+
 // out[0] = min key, out[1] = max key, out[2] = ROI count, out[3] = non-finite ROI count
-template <typename T, typename M>
+template <typename T, typename M, bool VEC>
 __global__ void __launch_bounds__(kDvhThreads) k_roi_stats(const T* __restrict__ dose, const M* __restrict__ mask,
                                                            long long n, unsigned long long* __restrict__ out) {
   unsigned long long kmin = ~0ull, kmax = 0ull, cnt = 0ull, bad = 0ull;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
-    if (!in_roi(mask, i)) continue;
-    const T x = __ldg(dose + i);
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  auto take = [&](T x) {
     ++cnt;
     if (!isfinite(x)) {
       ++bad;
-      continue;
+      return;
     }
     const unsigned long long k = order_key(x);
     kmin = min(kmin, k);
     kmax = max(kmax, k);
+  };
+  const long long n4 = n / 4;
+  for (long long q = tid; q < n4; q += stride) {
+    T x[4];
+    bool in[4];
+    load4<T, VEC>(dose, 4 * q, x);
+    roi4<M, VEC>(mask, 4 * q, in);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (in[k]) take(x[k]);
   }
+  for (long long i = 4 * n4 + tid; i < n; i += stride)
+    if (in_roi(mask, i)) take(__ldg(dose + i));
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     kmin = min(kmin, __shfl_xor_sync(0xffffffffu, kmin, o));
@@ -133,7 +178,7 @@ __device__ __forceinline__ int bin_of(T x, T first, T denom, T nb, int bins, con
 }
 
 // acc (nullable): ROI statistics of k_roi_stats; nothing is counted for an empty or non-finite ROI
-template <typename T, typename M, bool SMEM>
+template <typename T, typename M, bool SMEM, bool VEC>
 __global__ void __launch_bounds__(kDvhThreads) k_histogram(const T* __restrict__ dose, const M* __restrict__ mask,
                                                            long long n, const T* __restrict__ edges, int bins,
                                                            unsigned long long* __restrict__ counts,
@@ -147,16 +192,27 @@ __global__ void __launch_bounds__(kDvhThreads) k_histogram(const T* __restrict__
   const T first = __ldg(edges), last = __ldg(edges + bins);
   const T denom = sub_rn(last, first), nb = (T)bins;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
-    if (!in_roi(mask, i)) continue;
-    const T x = __ldg(dose + i);
-    if (!(x >= first && x <= last)) continue;  // numpy keeps [first, last] only
+  const long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  auto count = [&](T x) {
+    if (!(x >= first && x <= last)) return;  // numpy keeps [first, last] only
     const int b = bin_of<T>(x, first, denom, nb, bins, edges);
     if (SMEM)
       atomicAdd(h + b, 1u);
     else
       atomicAdd(counts + b, 1ull);
+  };
+  const long long n4 = n / 4;
+  for (long long q = tid; q < n4; q += stride) {
+    T x[4];
+    bool in[4];
+    load4<T, VEC>(dose, 4 * q, x);
+    roi4<M, VEC>(mask, 4 * q, in);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (in[k]) count(x[k]);
   }
+  for (long long i = 4 * n4 + tid; i < n; i += stride)
+    if (in_roi(mask, i)) count(__ldg(dose + i));
   if (SMEM) {
     __syncthreads();
     for (int b = threadIdx.x; b < bins; b += blockDim.x)
@@ -168,26 +224,47 @@ static int grid_for(long long n) {
   return (int)std::max<long long>(1, std::min<long long>((n + kDvhThreads - 1) / kDvhThreads, 152LL * 8));
 }
 
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+// vector loads when dose and mask start on 16-byte boundaries (4 voxels of the mask
+// span 4 or 16 bytes, and every group starts at a multiple of 4 voxels)
+static bool vec_ok(const void* dose, const void* mask) { return aligned16(dose) && (!mask || aligned16(mask)); }
+
 template <typename T, typename M>
 static void launch_stats(const void* dose, const void* mask, long long n, unsigned long long* out, cudaStream_t st) {
-  k_roi_stats<T, M><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n, out);
+  const int g = grid_for((n + 3) / 4);
+  if (vec_ok(dose, mask))
+    k_roi_stats<T, M, true><<<g, kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n, out);
+  else
+    k_roi_stats<T, M, false><<<g, kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n, out);
 }
 
 template <typename T, typename M>
 static void launch_hist(const void* dose, const void* mask, long long n, const void* edges, int bins,
                         unsigned long long* counts, cudaStream_t st, const unsigned long long* acc = nullptr) {
-  if (bins <= kSmemBins)
-    k_histogram<T, M, true><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n,
-                                                                  (const T*)edges, bins, counts, acc);
-  else
-    k_histogram<T, M, false><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n,
-                                                                   (const T*)edges, bins, counts, acc);
+  const int g = grid_for((n + 3) / 4);
+  const bool v = vec_ok(dose, mask);
+#define PVD_HIST(SM, VE)                                                                                     \
+  k_histogram<T, M, SM, VE><<<g, kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n, (const T*)edges, bins, \
+                                                       counts, acc)
+  if (bins <= kSmemBins) {
+    if (v)
+      PVD_HIST(true, true);
+    else
+      PVD_HIST(true, false);
+  } else {
+    if (v)
+      PVD_HIST(false, true);
+    else
+      PVD_HIST(false, false);
+  }
+#undef PVD_HIST
 }
 
 template <typename T, typename M>
 static void launch_dvh(const void* dose, const void* mask, long long n, int bins, void* edges,
                        unsigned long long* res, cudaStream_t st) {
-  k_roi_stats<T, M><<<grid_for(n), kDvhThreads, 0, st>>>((const T*)dose, (const M*)mask, n, res);
+  launch_stats<T, M>(dose, mask, n, res, st);
   k_dvh_edges<T><<<(bins + 256) / 256, 256, 0, st>>>(res, bins, (T*)edges);
   launch_hist<T, M>(dose, mask, n, edges, bins, res + 4, st, res);
 }

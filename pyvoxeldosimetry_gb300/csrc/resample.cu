@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256) k_prefilter(const float* __restrict__ src
                                                    int n1, int n2) {
   const int tx = threadIdx.x, ty = threadIdx.y;
   if constexpr (AXIS == 2) {
-    __shared__ float tile[kPfRows][kPfT2 + 2 * kFirHalf];
+    __shared__ __align__(16) float tile[kPfRows][kPfT2 + 2 * kFirHalf];  // rows of 160 floats: 16-byte aligned
     const long long rows = (long long)n0 * n1;
     const int x0 = blockIdx.x * kPfT2;
     const long long row = (long long)blockIdx.y * kPfRows + ty;
@@ -72,13 +72,21 @@ __global__ void __launch_bounds__(256) k_prefilter(const float* __restrict__ src
       tile[ty][c] = row_ok ? __ldg(in + mirror_index(x0 - kFirHalf + c, n2)) : 0.0f;
     __syncthreads();
     if (!row_ok) return;
-    for (int c = tx; c < kPfT2; c += 32) {
-      const int x = x0 + c;
-      if (x >= n2) break;
-      const float* t = &tile[ty][c + kFirHalf];
-      float acc = c_fir[0] * t[0];
+    // 4 consecutive outputs per thread from one 36-sample window (nine 16-byte reads)
+    constexpr int OX = kPfT2 / 32;  // 4
+    float win[OX + 2 * kFirHalf];
 #pragma unroll
-      for (int k = 1; k <= kFirHalf; ++k) acc += c_fir[k] * (t[-k] + t[k]);
+    for (int q = 0; q < (OX + 2 * kFirHalf) / 4; ++q) {
+      const float4 v = *reinterpret_cast<const float4*>(&tile[ty][tx * OX + 4 * q]);
+      win[4 * q] = v.x, win[4 * q + 1] = v.y, win[4 * q + 2] = v.z, win[4 * q + 3] = v.w;
+    }
+#pragma unroll
+    for (int o = 0; o < OX; ++o) {
+      const int x = x0 + tx * OX + o;
+      if (x >= n2) break;
+      float acc = c_fir[0] * win[o + kFirHalf];
+#pragma unroll
+      for (int k = 1; k <= kFirHalf; ++k) acc += c_fir[k] * (win[o + kFirHalf - k] + win[o + kFirHalf + k]);
       out[row * n2 + x] = acc;
     }
   } else {
@@ -94,12 +102,18 @@ __global__ void __launch_bounds__(256) k_prefilter(const float* __restrict__ src
       tile[r][tx] = x_ok ? __ldg(src + base + (long long)mirror_index(a0 - kFirHalf + r, n) * stride) : 0.0f;
     __syncthreads();
     if (!x_ok) return;
-    for (int r = ty; r < kPfT; r += blockDim.y) {
-      const int i = a0 + r;
-      if (i >= n) break;
-      float acc = c_fir[0] * tile[r + kFirHalf][tx];
+    // 8 consecutive outputs per thread from one 40-sample window of its column
+    constexpr int OY = kPfT / kPfRows;  // 8
+    float win[OY + 2 * kFirHalf];
 #pragma unroll
-      for (int k = 1; k <= kFirHalf; ++k) acc += c_fir[k] * (tile[r + kFirHalf - k][tx] + tile[r + kFirHalf + k][tx]);
+    for (int k = 0; k < OY + 2 * kFirHalf; ++k) win[k] = tile[ty * OY + k][tx];
+#pragma unroll
+    for (int o = 0; o < OY; ++o) {
+      const int i = a0 + ty * OY + o;
+      if (i >= n) break;
+      float acc = c_fir[0] * win[o + kFirHalf];
+#pragma unroll
+      for (int k = 1; k <= kFirHalf; ++k) acc += c_fir[k] * (win[o + kFirHalf - k] + win[o + kFirHalf + k]);
       out[base + (long long)i * stride] = acc;
     }
   }
