@@ -153,3 +153,28 @@ def test_batch_fit_never_feeds_a_non_finite_value_to_the_convolution():
     assert not ok[[1, 3, 4]].any()
     assert ok[5:].mean() > 0.99
     bc.close()
+
+
+@pytest.mark.parametrize("times", [[1.0, 4.0, 24.0, 48.0, 96.0],
+                                   [0.5, 1.0, 2.0, 4.0, 8.0, 16.0, 24.0, 48.0, 72.0, 96.0]])
+def test_batch_fit_with_more_timepoints(times):
+    """5 samples (register arrays of 6) and 10 samples (arrays of 16): the projected fit
+    recovers the analytic cumulated activity of noise-free two-exponential curves."""
+    from pyvoxeldosimetry_gb300.batch import BatchDoseCalculator
+    shape = (24, 20, 28)
+    rng = np.random.default_rng(len(times))
+    a0 = rng.random(shape) ** 2 * 1e5 + 10.0
+    k1 = np.log(2) / np.exp(rng.uniform(np.log(6), np.log(160), shape))
+    k2 = np.log(2) / np.exp(rng.uniform(np.log(6), np.log(160), shape))
+    w = rng.uniform(0.2, 0.8, shape)
+    acts = np.stack([a0 * (w * np.exp(-k1 * t) + (1 - w) * np.exp(-k2 * t)) for t in times]).astype(np.float32)
+    auc = (a0 * (w / k1 + (1 - w) / k2)).reshape(-1)
+    bc = BatchDoseCalculator("Lu177", use_graph=False)
+    d = bc.calculate([{"activity": torch.from_numpy(acts).cuda(), "times": times, "voxel_size": (2.0,) * 3}])[0]
+    _, fa, ok = bc.fit_results(0)
+    ok = ok.view(-1).cpu().numpy()
+    rel = np.abs(fa.view(-1).cpu().numpy() - auc) / auc
+    assert ok.mean() > 0.99
+    assert np.median(rel[ok]) < 1e-6 and np.quantile(rel[ok], 0.99) < 1e-3
+    assert torch.isfinite(d).all()
+    bc.close()

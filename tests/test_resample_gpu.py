@@ -108,3 +108,22 @@ def test_direct_and_separable_entry_points_agree(order):
     with pytest.raises(N.PvdError):
         N.check(lib.pvd_resample_separable(src.data_ptr(), *shape, b.data_ptr(), *m, st3, or3, order, 2.0,
                                            scr.data_ptr(), n_scr - 1, sh))
+
+
+def test_fixed_resolution_kernel_with_density():
+    """The density map is resampled to the kernel grid (trilinear, no volume scaling) and
+    used there; the pipeline equals the oracle's resample -> conv / rho -> resample."""
+    from pyvoxeldosimetry_gb300.core.kernel_convolution import KernelConvolutionCalculator
+    rng = np.random.default_rng(21)
+    act = (rng.random((24, 22, 26)) ** 3 * 1e5).astype(np.float32)
+    rho = rng.uniform(0.5, 1.5, act.shape).astype(np.float32)
+    idx = np.indices((7, 7, 7)) - 3.0
+    k = np.exp(-np.sqrt((idx ** 2).sum(0)) / 1.8) / np.maximum(np.sqrt((idx ** 2).sum(0)), 0.62) ** 2
+    vs, kr = (1.5, 1.5, 1.5), 2.0
+    calc = KernelConvolutionCalculator("Y90", kernel_resolution=kr, config={"kernel": k, "autotune": False})
+    d = calc.calculate_dose_rate(act, vs, density=rho)
+    a2 = ors.resample(act, vs, (kr,) * 3, conserve_total=True)
+    r2 = ors.resample(rho, vs, (kr,) * 3, order=1)
+    d2 = oc.density_scale(oc.linear_conv_same(a2, k), r2)
+    ref = ors.resample(d2, (kr,) * 3, vs, output_shape=act.shape)
+    assert np.abs(d - ref).max() <= 1e-4 * np.abs(ref).max()
