@@ -630,7 +630,7 @@ def main():
                        "wall_ms_per_step": 1e3 * wall / args.steps,
                        "api": "KernelConvolutionCalculator.calculate_dose_rate(pinned CPU tensors)"}
 
-    if not args.no_extras:
+    if not args.no_extras and rank == 0:  # sub-measurements of one GPU; only rank 0 prints
         line["mc"] = measure_mc(device)
         line["tac_fit"] = measure_fit(device)
         line["tac_fit_vp"] = measure_vp_fit(device)
