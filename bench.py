@@ -403,6 +403,106 @@ def measure_resample(device, shape=(256, 256, 256), reps=5):
             "workload": "resample_volume order 3, 256^3 float32, whole call"}
 
 
+def measure_unet(device, small=False, train_steps=20, reps=3):
+    """Learned correction: one training step (forward, both gradients, Adam) on a
+    64^3 crop, NN-corrected dose (plain density-scaled convolution + U-Net +
+    apply) of a 128^3 CT-like phantom at 3 mm, and the GPU Monte Carlo run to 1 %
+    statistical uncertainty on the same phantom (median relative standard error
+    over voxels above 10 % of the maximum, from 10 independent batches)."""
+    import torch
+    from pyvoxeldosimetry_gb300 import phantoms
+    from pyvoxeldosimetry_gb300.core import learned_correction as lc
+    from pyvoxeldosimetry_gb300.core.kernel_convolution import KernelConvolutionCalculator
+    from pyvoxeldosimetry_gb300.core.monte_carlo import McPlan, physics_tables
+    peaks = load_peaks()
+    tc_peak = peaks.get("bf16_tflops", 1900.0)
+    shape = (64, 64, 64) if small else (128, 128, 128)
+    crop = (32, 32, 32) if small else (64, 64, 64)
+    vox = (3.0, 3.0, 3.0)
+    act, rho = phantoms.ct_phantom(shape, 3.0, seed=7)
+    a = torch.from_numpy(act).to(device)
+    r = torch.from_numpy(rho).to(device)
+    conv = KernelConvolutionCalculator("Y90")
+    dc = conv.calculate_dose_rate(a, vox, density=r)
+    dcn = dc.cpu().numpy()
+    pair = lc.make_pair(act, rho, dcn, dcn * 1.1, device=device)
+    net = lc.UNet3D(seed=1, device=device)
+    lc.train(net, [pair], 3, crop=crop)
+    s = torch.cuda.current_stream().cuda_stream
+    ws = net.workspace(crop, train=True)
+
+    def one_step():
+        net.pack_input(ws, (pair.activity, pair.density, pair.dose_conv), pair.scales, (0, 0, 0), s)
+        net.forward(ws, s)
+        net.backward(ws, pair.target, pair.weight, (0, 0, 0), s)
+        net.adam(lr=1e-4)
+
+    one_step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(train_steps):
+        one_step()
+    e1.record()
+    e1.synchronize()
+    step_ms = e0.elapsed_time(e1) / train_steps
+    # forward + data gradient (all but the first layer) + weight gradient
+    fwd = lc.conv_flops(crop)
+    first = 2.0 * 27 * 16 * 16 * crop[0] * crop[1] * crop[2]
+    step_flops = 3 * fwd - first
+    # inference: plain conv + network + apply on the whole phantom
+    out = torch.empty_like(dc)
+    lc.predict(net, a, r, dc, out=out)
+    inf_ms, conv_ms = [], []
+    for _ in range(reps):
+        e0.record()
+        d = conv.calculate_dose_rate(a, vox, density=r)
+        e1.record()
+        e1.synchronize()
+        conv_ms.append(e0.elapsed_time(e1))
+        e0.record()
+        lc.predict(net, a, r, d, out=out)
+        e1.record()
+        e1.synchronize()
+        inf_ms.append(e0.elapsed_time(e1))
+    conv_t, inf_t = float(np.median(conv_ms)), float(np.median(inf_ms))
+    infer_crop = tuple(-(-n // 8) * 8 for n in shape)
+    nvox = float(np.prod(shape))
+    # Monte Carlo to 1 %: 10 batches, relative standard error of the mean per voxel
+    plan = McPlan(shape, vox, physics_tables("Y90"), device)
+    hb = 2_000_000 if small else 10_000_000
+    batches = []
+    e0.record()
+    for b in range(10):
+        _, dr, _ = plan.run(a, r, hb, 1000 + b, dose=True)
+        batches.append(dr.cpu().numpy().astype(np.float64))
+    e1.record()
+    e1.synchronize()
+    mc_ms = e0.elapsed_time(e1)
+    plan.close()
+    conv.close()
+    st = np.stack(batches)
+    mean = st.mean(0)
+    sel = mean > 0.1 * mean.max()
+    rse = st.std(0, ddof=1)[sel] / np.sqrt(10) / mean[sel]
+    rse_med = float(np.median(rse))
+    mc_1pct_ms = mc_ms * (rse_med / 0.01) ** 2
+    nn_ms = conv_t + inf_t
+    return {
+        "value": nvox / (nn_ms / 1e3) / 1e9, "unit": "Gvoxel/s (NN-corrected dose)",
+        "workload": f"Y-90, {list(shape)} CT-like phantom at 3 mm: density-scaled conv + U-Net "
+                    f"(4 levels, 16-128 ch) + apply; training step on a {list(crop)} crop",
+        "plain_conv_ms": conv_t, "unet_inference_ms": inf_t, "nn_corrected_ms": nn_ms,
+        "plain_conv_gvox_s": nvox / (conv_t / 1e3) / 1e9,
+        "unet_inference_tflops": lc.conv_flops(infer_crop) / (inf_t / 1e3) / 1e12,
+        "train_step_ms": step_ms, "train_step_tflops": step_flops / (step_ms / 1e3) / 1e12,
+        "train_tensor_frac": step_flops / (step_ms / 1e3) / 1e12 / tc_peak,
+        "tensor_peak_tflops": tc_peak,
+        "mc_histories_per_batch": hb, "mc_ms_10_batches": mc_ms, "mc_median_rel_se": rse_med,
+        "mc_to_1pct_ms": mc_1pct_ms, "nn_vs_mc_1pct_speedup": mc_1pct_ms / nn_ms,
+    }
+
+
 def run_only(args, device):
     """One sub-measurement alone (a bounded case to profile), printed as its own JSON line."""
     small = args.small
@@ -416,6 +516,8 @@ def run_only(args, device):
         r = measure_dvh(device, shape=(128, 128, 128) if small else (256, 256, 256))
     elif args.only == "vpfit":
         r = measure_vp_fit(device, shape=(64, 128, 128) if small else (256, 256, 256))
+    elif args.only == "unet":
+        r = measure_unet(device, small=small)
     else:
         r = measure_batch(device, 2 if small else args.batch_volumes)
     print(json.dumps({"only": args.only, "small": small, **r}), flush=True)
@@ -499,7 +601,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the MC, fit and batch sub-measurements")
     ap.add_argument("--batch-volumes", type=int, default=8,
                     help="volumes of the 64-volume seeded uneven batch to run in the batch sub-measurement")
-    ap.add_argument("--only", choices=["mc", "fit", "vpfit", "batch", "dvh", "resample"],
+    ap.add_argument("--only", choices=["mc", "fit", "vpfit", "batch", "dvh", "resample", "unet"],
                     help="run one sub-measurement alone and print it (no contract line)")
     ap.add_argument("--small", action="store_true", help="with --only: a bounded case for profiling")
     args = ap.parse_args()
@@ -637,6 +739,7 @@ def main():
         line["batch"] = measure_batch(device, args.batch_volumes)
         line["dvh"] = measure_dvh(device)
         line["resample"] = measure_resample(device)
+        line["unet"] = measure_unet(device)
 
     if rank == 0 and not args.no_cpu_baseline:
         ks = reference_kernels(wl)

@@ -472,6 +472,127 @@ pvd_status pvd_radial_kernel(const pvd_radial_term* terms, int n_terms, double s
                              const double* voxel_mm, double* out_d, pvd_stream stream);
 
 /* ------------------------------------------------------------------------ */
+/* Learned heterogeneity correction: 3-D U-Net layers on tcgen05 (BF16, FP32   */
+/* accumulation)                                                              */
+/* ------------------------------------------------------------------------ */
+/* No counterpart in the reference, whose correction of the water kernel for
+ * tissue heterogeneity is the unused `tissue_densities` hook
+ * (core/dose_calculator.py:90) and whose Monte Carlo cannot run
+ * (core/monte_carlo.py:38-40).  These calls are the layers of a small 3-D
+ * U-Net that predicts log(D_MC / D_conv) from activity, density and the
+ * convolution dose; the network is trained on pairs produced by pvd_mc_run and
+ * pvd_conv_execute.
+ *
+ * Tensor layout ("plane" layout): a tensor of C channels (C a multiple of 16
+ * for convolutions, of 8 elsewhere) on a D x H x W grid is C/8 planes of
+ * `rows` rows x 8 BF16 values (16 bytes per row), planes `rows * 16` bytes
+ * apart.  Row `margin + p` holds voxel p of the zero-haloed grid
+ * (D+2) x (H+2) x (W+2) flattened in C order.  Halo and margin rows must be
+ * zero when a tensor is first used (allocate zeroed); every call here keeps
+ * them zero.  A channel concatenation is two tensors whose planes are
+ * adjacent in one allocation. */
+typedef struct {
+  int dims[3];          /* D, H, W interior voxels */
+  int64_t padded;       /* (D+2)(H+2)(W+2) */
+  int64_t padded_tiles; /* padded rounded up to a multiple of 128 */
+  int64_t margin;       /* zero rows before (and after) the padded grid */
+  int64_t rows;         /* rows of one plane: 2 * margin + padded_tiles */
+} pvd_unet_geom;
+
+enum {
+  PVD_UNET_ACT_LEAKY = 1, /* apply LeakyReLU(slope) after the bias */
+  PVD_UNET_ACCUMULATE = 2 /* add the result to the output tensor's contents */
+};
+
+pvd_status pvd_unet_geometry(int d, int h, int w, pvd_unet_geom* out);
+
+/* 3x3x3 convolution, zero padding 1, as implicit GEMM on the tensor cores:
+ *   y[v][n] = act( bias[n] + sum_{tap,k} x[v + tap][k] * W[n][k][tap] )
+ *             * (mask ? leaky'(mask[v][n]) : 1)  (+ y[v][n] if ACCUMULATE)
+ * with w_packed from pvd_unet_pack_weights (forward layout).  The same call
+ * with the data-gradient layout, x = output gradient and mask = the layer's
+ * input gives the input gradient times the previous LeakyReLU's derivative.
+ * cin, cout: multiples of 16 in [16, 256]; bias may be NULL. */
+pvd_status pvd_unet_conv3d(const pvd_unet_geom* geom, const void* x, int cin, const void* w_packed, const float* bias,
+                           void* y, int cout, const void* mask, int flags, float slope, pvd_stream stream);
+
+/* dw[n][k][tap] (+)= sum_v x[v + tap][k] * grad[v][n]  (FP32 [cout][cin][27],
+ * the torch conv3d weight layout).  Deterministic: split over voxels on the
+ * tensor cores, partial sums added in a fixed order.  workspace: device
+ * memory of at least pvd_unet_wgrad_workspace bytes. */
+pvd_status pvd_unet_wgrad_workspace(const pvd_unet_geom* geom, int cin, int cout, size_t* bytes);
+pvd_status pvd_unet_conv3d_wgrad(const pvd_unet_geom* geom, const void* x, int cin, const void* grad, int cout,
+                                 float* dw, int accumulate, void* workspace, size_t workspace_bytes,
+                                 pvd_stream stream);
+
+/* FP32 weights [cout][cin][27] -> BF16 forward layout [27][cin/8][cout][8]
+ * (fwd_packed) and data-gradient layout [27][cout/8][cin][8] with mirrored
+ * taps (bwd_packed); either output may be NULL. */
+pvd_status pvd_unet_pack_weights(const float* w, int cin, int cout, void* fwd_packed, void* bwd_packed,
+                                 pvd_stream stream);
+
+/* Network input (16 channels): channel c < n_in (<= 4) is volumes[c] (device
+ * float32, C order, vol_dims) read at origin + voxel, times scales[c], then
+ * modes[c]: 0 linear, 1 sqrt, 2 log1p; channels >= n_in are zero, and so is
+ * every channel of a voxel outside the volumes (a crop may overhang them). */
+pvd_status pvd_unet_pack_input(const pvd_unet_geom* geom, const float* const* volumes, const float* scales,
+                               const int* modes, int n_in, const int* vol_dims, const int* origin, void* x,
+                               pvd_stream stream);
+
+/* 2x2x2 average pooling (fine dims = 2 x coarse dims) and its backward:
+ * dx = ((accumulate ? dx : 0) + dy[parent] / 8) * (mask ? leaky'(mask) : 1). */
+pvd_status pvd_unet_pool(const pvd_unet_geom* fine, const void* x, const pvd_unet_geom* coarse, void* y, int channels,
+                         pvd_stream stream);
+pvd_status pvd_unet_pool_backward(const pvd_unet_geom* coarse, const void* dy, const pvd_unet_geom* fine, void* dx,
+                                  const void* mask, int channels, int accumulate, float slope, pvd_stream stream);
+
+/* Nearest-neighbour 2x upsampling and its backward: dx = (sum of the 8
+ * children of dy) * (mask ? leaky'(mask) : 1). */
+pvd_status pvd_unet_upsample(const pvd_unet_geom* coarse, const void* x, const pvd_unet_geom* fine, void* y,
+                             int channels, pvd_stream stream);
+pvd_status pvd_unet_upsample_backward(const pvd_unet_geom* fine, const void* dy, const pvd_unet_geom* coarse, void* dx,
+                                      const void* mask, int channels, float slope, pvd_stream stream);
+
+/* Output head (1x1x1, 16 -> 2): out[0][v] = mu (predicted log(D_MC/D_conv)),
+ * out[1][v] = s (predicted log of its squared error); w_head = [w_mu(16),
+ * w_s(16), b_mu, b_s]; out: device float32 [2][D][H][W]. */
+pvd_status pvd_unet_head(const pvd_unet_geom* geom, const void* x, const float* w_head, float* out, pvd_stream stream);
+
+/* Loss and head backward.  target, weight: device float32 volumes of vol_dims
+ * read at origin (voxels outside them have weight 0).  With e = mu - target and l = log(e^2 + eps):
+ *   loss_mu = sum weight e^2 / n,  loss_s = sum weight (s - l)^2 / n
+ * (n = D*H*W; l treated as a constant).  Writes grad_x (16-channel tensor: the
+ * gradient at the head input times leaky'(x)) and grads_and_loss[36] =
+ * [d w_mu (16), d w_s (16), d b_mu, d b_s, loss_mu, loss_s]. */
+pvd_status pvd_unet_head_loss_workspace(const pvd_unet_geom* geom, size_t* bytes);
+pvd_status pvd_unet_head_loss(const pvd_unet_geom* geom, const void* x, const float* w_head, const float* pred,
+                              const float* target, const float* weight, const int* vol_dims, const int* origin,
+                              float eps, float slope, void* grad_x, float* grads_and_loss, void* workspace,
+                              size_t workspace_bytes, pvd_stream stream);
+
+/* Corrected dose on the volume voxels that the crop at `origin` covers:
+ * dose_out[v] = dose_conv[v] * exp(clamp(mu, +-mu_clamp)), or dose_conv[v]
+ * itself (fallback[v] = 1, if fallback is not NULL) where the predicted error
+ * sqrt(exp(s)) exceeds sigma_max or is not finite.  pred from pvd_unet_head. */
+pvd_status pvd_unet_apply_correction(const pvd_unet_geom* geom, const float* pred, const float* dose_conv,
+                                     const int* vol_dims, const int* origin, float sigma_max, float mu_clamp,
+                                     float* dose_out, uint8_t* fallback, pvd_stream stream);
+
+/* db[c] = sum over interior voxels of grad[v][c] (fixed-order reduction). */
+pvd_status pvd_unet_bias_grad_workspace(const pvd_unet_geom* geom, int channels, size_t* bytes);
+pvd_status pvd_unet_bias_grad(const pvd_unet_geom* geom, const void* grad, int channels, float* db, void* workspace,
+                              size_t workspace_bytes, pvd_stream stream);
+
+/* Adam (bias-corrected, decoupled weight decay) on n FP32 parameters; step >= 1. */
+pvd_status pvd_adam_step(float* params, const float* grads, float* m, float* v, int64_t n, float lr, float beta1,
+                         float beta2, float eps, float weight_decay, int step, pvd_stream stream);
+
+/* First failure code recorded by a U-Net kernel (0: none; a bounded wait of
+ * the tensor-core pipeline ran out otherwise, and PVD_ERR_TIMEOUT is
+ * returned).  Synchronises the device; reset != 0 clears it. */
+pvd_status pvd_unet_status(int* code, int reset);
+
+/* ------------------------------------------------------------------------ */
 /* Misc                                                                       */
 /* ------------------------------------------------------------------------ */
 

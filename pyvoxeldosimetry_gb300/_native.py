@@ -45,6 +45,11 @@ EXPORTED_SYMBOLS = [
     "pvd_roi_stats", "pvd_histogram", "pvd_dvh",
     "pvd_bspline_prefilter", "pvd_resample", "pvd_resample_separable",
     "pvd_radial_kernel",
+    "pvd_unet_geometry", "pvd_unet_conv3d", "pvd_unet_wgrad_workspace", "pvd_unet_conv3d_wgrad",
+    "pvd_unet_pack_weights", "pvd_unet_pack_input", "pvd_unet_pool", "pvd_unet_pool_backward",
+    "pvd_unet_upsample", "pvd_unet_upsample_backward", "pvd_unet_head", "pvd_unet_head_loss_workspace",
+    "pvd_unet_head_loss", "pvd_unet_apply_correction", "pvd_unet_bias_grad_workspace", "pvd_unet_bias_grad", "pvd_adam_step",
+    "pvd_unet_status",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
 ]
 
@@ -94,6 +99,14 @@ class RadialTerm(C.Structure):
 PVD_TERM_COLE, PVD_TERM_PHOTON, PVD_TERM_ALPHA, PVD_TERM_EXP_R2 = 0, 1, 2, 3
 PVD_CENTER_R0, PVD_CENTER_ZERO, PVD_CENTER_NAN = 0, 1, 2
 PVD_MAX_RADIAL_TERMS = 16
+
+
+class UnetGeom(C.Structure):
+    _fields_ = [("dims", C.c_int * 3), ("padded", C.c_int64), ("padded_tiles", C.c_int64),
+                ("margin", C.c_int64), ("rows", C.c_int64)]
+
+
+PVD_UNET_ACT_LEAKY, PVD_UNET_ACCUMULATE = 1, 2
 
 
 class PlanInfo(C.Structure):
@@ -158,6 +171,27 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_resample": (st, [vp, i, i, i, vp, i, i, i, C.POINTER(C.c_double), C.POINTER(C.c_double), i, f, vp]),
         "pvd_resample_separable": (st, [vp, i, i, i, vp, i, i, i, C.POINTER(C.c_double), C.POINTER(C.c_double), i, f,
                                         vp, C.c_longlong, vp]),
+        "pvd_unet_geometry": (st, [i, i, i, C.POINTER(UnetGeom)]),
+        "pvd_unet_conv3d": (st, [C.POINTER(UnetGeom), vp, i, vp, vp, vp, i, vp, i, f, vp]),
+        "pvd_unet_wgrad_workspace": (st, [C.POINTER(UnetGeom), i, i, C.POINTER(C.c_size_t)]),
+        "pvd_unet_conv3d_wgrad": (st, [C.POINTER(UnetGeom), vp, i, vp, i, vp, i, vp, C.c_size_t, vp]),
+        "pvd_unet_pack_weights": (st, [vp, i, i, vp, vp, vp]),
+        "pvd_unet_pack_input": (st, [C.POINTER(UnetGeom), C.POINTER(vp), C.POINTER(f), C.POINTER(i), i,
+                                     C.POINTER(i), C.POINTER(i), vp, vp]),
+        "pvd_unet_pool": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), vp, i, vp]),
+        "pvd_unet_pool_backward": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), vp, vp, i, i, f, vp]),
+        "pvd_unet_upsample": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), vp, i, vp]),
+        "pvd_unet_upsample_backward": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), vp, vp, i, f, vp]),
+        "pvd_unet_head": (st, [C.POINTER(UnetGeom), vp, vp, vp, vp]),
+        "pvd_unet_head_loss_workspace": (st, [C.POINTER(UnetGeom), C.POINTER(C.c_size_t)]),
+        "pvd_unet_head_loss": (st, [C.POINTER(UnetGeom), vp, vp, vp, vp, vp, C.POINTER(i), C.POINTER(i), f, f, vp,
+                                    vp, vp, C.c_size_t, vp]),
+        "pvd_unet_apply_correction": (st, [C.POINTER(UnetGeom), vp, vp, C.POINTER(i), C.POINTER(i), f, f, vp, vp,
+                                           vp]),
+        "pvd_unet_bias_grad_workspace": (st, [C.POINTER(UnetGeom), i, C.POINTER(C.c_size_t)]),
+        "pvd_unet_bias_grad": (st, [C.POINTER(UnetGeom), vp, i, vp, vp, C.c_size_t, vp]),
+        "pvd_adam_step": (st, [vp, vp, vp, vp, C.c_int64, f, f, f, f, f, i, vp]),
+        "pvd_unet_status": (st, [C.POINTER(i), i]),
         "pvd_last_error": (st, [C.c_char_p, C.c_size_t]),
         "pvd_version": (i, []),
         "pvd_launch_count": (C.c_uint64, [i]),

@@ -33,7 +33,7 @@ from .activity_sampler import SECONDS_PER, ActivitySampler
 from .kernel_convolution import KernelConvolutionCalculator
 
 METHODS = {"kernel": "kernel", "kernel_convolution": "kernel", "gpu_monte_carlo": "monte_carlo",
-           "monte_carlo": "monte_carlo", "gate_monte_carlo": "gate"}
+           "monte_carlo": "monte_carlo", "gate_monte_carlo": "gate", "nn_corrected": "nn_corrected"}
 
 
 @dataclass
@@ -67,6 +67,10 @@ class DoseCalculator:
                 n_particles=self.config.get("n_particles", 1000000),
                 random_seed=self.config.get("random_seed", None),
                 config=self.config)
+        elif kind == "nn_corrected":
+            from .learned_correction import NNCorrectedDoseCalculator
+            self.calculator = NNCorrectedDoseCalculator(radionuclide, self.config.get("tissue_composition", None),
+                                                        self.config)
         elif kind == "gate":
             raise NotImplementedError("gate_monte_carlo drives the external GATE/Geant4 application, which this "
                                       "package does not provide; use method='monte_carlo'")

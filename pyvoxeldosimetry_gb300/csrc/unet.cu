@@ -1,0 +1,1101 @@
+// Learned heterogeneity correction: the 3-D U-Net's BF16 training and inference
+// kernels on the fifth-generation tensor cores (tcgen05, FP32 accumulation in
+// tensor memory), plus the memory-bound layers around them.
+//
+// Activation layout ("plane" layout): a tensor of C channels (C a multiple of
+// 16) on a D x H x W grid is C/8 planes; a plane is `rows` rows of 16 bytes
+// (8 BF16 channels of one voxel).  Rows index the zero-haloed grid
+// (D+2) x (H+2) x (W+2) flattened in C order, offset by `margin` zero rows on
+// both sides.  Halo and margin rows are zero in every tensor, so a 3x3x3 tap is
+// a constant row offset and a tile of 128 consecutive rows of one tap is one
+// contiguous 2 KB block per plane - exactly the no-swizzle core-matrix layout
+// the tensor core reads (8 rows x 16 bytes per core matrix).
+//
+// Convolution as implicit GEMM (forward and data gradient):
+//   Y[p, n] = sum_{tap, k} X[p + off(tap), k] * Wt[tap][n][k]   (M = 128 rows p,
+//   N = output channels, K = 27 x input channels), one tcgen05.mma per 16 K.
+// For each (dz, dy) the CTA stages a 130-row slab per plane; the three dx taps
+// read it at row offsets 0, 1, 2 (descriptor start +16 bytes each).
+// Weight gradient: dW[tap][k][n] = sum_p X[p + off(tap), k] G[p, n]: M = 128
+// (tap, input-channel) pairs, N = output channels, K = rows, both operands
+// MN-major straight from the plane layout; split over rows, partial sums
+// reduced in a fixed order (deterministic).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <string>
+
+#include "pvd_common.cuh"
+#include "umma.cuh"
+
+namespace pvd {
+namespace unet {
+
+constexpr int TILE_M = 128;
+constexpr int SLAB_ROWS = TILE_M + 2;
+constexpr uint32_t SLAB_PITCH = SLAB_ROWS * 16;  // bytes of one plane's slab
+constexpr int WG_KT = 64;                        // rows per weight-gradient stage
+constexpr uint64_t WAIT_NS = 2000000000ull;      // bound of every mbarrier wait (2 s)
+constexpr int CONV_THREADS = 192;                // warp 0 loads, warp 1 MMA, warps 2-5 epilogue
+constexpr int MAX_SMEM = 232448;                 // 227 KB opt-in dynamic shared memory
+
+enum { ST_TIMEOUT_LOAD = 1, ST_TIMEOUT_MMA = 2, ST_TIMEOUT_EPI = 3 };
+
+__device__ int g_unet_status;  // first failure code seen by any kernel (0 = none)
+
+__device__ __forceinline__ void fail(int code) { atomicCAS(&g_unet_status, 0, code); }
+
+struct Geo {
+  int D, H, W, Hp, Wp;
+  long long np, np_tiles, margin, rows;
+};
+
+static Geo make_geo(const pvd_unet_geom* g) {
+  Geo o;
+  o.D = g->dims[0];
+  o.H = g->dims[1];
+  o.W = g->dims[2];
+  o.Hp = o.H + 2;
+  o.Wp = o.W + 2;
+  o.np = g->padded;
+  o.np_tiles = g->padded_tiles;
+  o.margin = g->margin;
+  o.rows = g->rows;
+  return o;
+}
+
+__device__ __forceinline__ bool interior(const Geo& g, long long p) {
+  if (p >= g.np) return false;
+  int x = (int)(p % g.Wp);
+  long long t = p / g.Wp;
+  int y = (int)(t % g.Hp);
+  int z = (int)(t / g.Hp);
+  return x >= 1 && x <= g.W && y >= 1 && y <= g.H && z >= 1 && z <= g.D;
+}
+
+__device__ __forceinline__ long long tap_offset(const Geo& g, int tap) {
+  int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;
+  return (long long)(dz - 1) * g.Hp * g.Wp + (long long)(dy - 1) * g.Wp + (dx - 1);
+}
+
+__device__ __forceinline__ float leaky_grad(float m, float slope) { return m > 0.f ? 1.f : slope; }
+
+__device__ __forceinline__ void unpack8(uint4 u, float* f) {
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float2 t = __bfloat1622float2(h[i]);
+    f[2 * i] = t.x;
+    f[2 * i + 1] = t.y;
+  }
+}
+__device__ __forceinline__ uint4 pack8(const float* f) {
+  uint4 u;
+  __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(&u);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+  return u;
+}
+
+// ---------------------------------------------------------------------------
+// 3x3x3 convolution (forward / data gradient), persistent, warp-specialised
+// ---------------------------------------------------------------------------
+struct ConvArgs {
+  const uint8_t* x;     // input plane 0
+  const uint8_t* w;     // packed weights [27][cin/8][cout][8] BF16
+  const float* bias;    // [cout] or null
+  uint8_t* y;           // output plane 0
+  const uint8_t* mask;  // plane 0 of a cout-channel tensor whose LeakyReLU derivative scales the result, or null
+  int cin, cout, flags, nb, n_tiles;
+  float slope;
+  long long plane;  // bytes per plane (rows * 16), same for x, y, mask
+  Geo g;
+};
+
+__global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  const int cin8 = a.cin >> 3;
+  const uint32_t a_bytes = (uint32_t)cin8 * SLAB_PITCH;
+  const uint32_t b_bytes = (uint32_t)a.cin * a.cout * 2;
+  const int nb = a.nb;
+  uint8_t* sa = sm;
+  uint8_t* sb = sm + 2 * a_bytes;
+  uint64_t* full_a = reinterpret_cast<uint64_t*>(sb + (size_t)nb * b_bytes);
+  uint64_t* empty_a = full_a + 2;
+  uint64_t* full_b = empty_a + 2;
+  uint64_t* empty_b = full_b + nb;
+  uint64_t* acc_full = empty_b + nb;
+  uint64_t* acc_empty = acc_full + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ncols = umma::tmem_cols(2 * a.cout);
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&full_a[i], 1);
+      mbar_init(&empty_a[i], 1);
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], 128);
+    }
+    for (int i = 0; i < nb; ++i) {
+      mbar_init(&full_b[i], 1);
+      mbar_init(&empty_b[i], 1);
+    }
+    fence_mbar_init();
+  }
+  if (warp == 1) umma::tmem_alloc(tslot, ncols);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const Geo& g = a.g;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it_a = 0, it_b = 0;
+      for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+        const long long p0 = (long long)tile * TILE_M;
+        for (int grp = 0; grp < 9; ++grp) {
+          const int dz = grp / 3, dy = grp % 3;
+          const long long row0 = g.margin + p0 + (long long)(dz - 1) * g.Hp * g.Wp + (long long)(dy - 1) * g.Wp - 1;
+          const int s = it_a & 1;
+          if (!mbar_wait_bounded(&empty_a[s], ((it_a >> 1) & 1) ^ 1, WAIT_NS)) {
+            fail(ST_TIMEOUT_LOAD);
+            goto done;
+          }
+          mbar_arrive_expect_tx(&full_a[s], a_bytes);
+          for (int c = 0; c < cin8; ++c)
+            umma::bulk_g2s(sa + (size_t)s * a_bytes + (size_t)c * SLAB_PITCH, a.x + c * a.plane + row0 * 16, SLAB_PITCH,
+                           &full_a[s]);
+          ++it_a;
+          for (int dx = 0; dx < 3; ++dx) {
+            const int tap = grp * 3 + dx;
+            const int sbi = it_b % nb;
+            if (!mbar_wait_bounded(&empty_b[sbi], ((it_b / nb) & 1) ^ 1, WAIT_NS)) {
+              fail(ST_TIMEOUT_LOAD);
+              goto done;
+            }
+            mbar_arrive_expect_tx(&full_b[sbi], b_bytes);
+            umma::bulk_g2s(sb + (size_t)sbi * b_bytes, a.w + (size_t)tap * b_bytes, b_bytes, &full_b[sbi]);
+            ++it_b;
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = umma::idesc_bf16(a.cout, false, false);
+      const uint32_t b_lbo = (uint32_t)a.cout * 16;
+      int it_a = 0, it_b = 0, t_local = 0;
+      for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++t_local) {
+        const int acc = t_local & 1;
+        if (!mbar_wait_bounded(&acc_empty[acc], ((t_local >> 1) & 1) ^ 1, WAIT_NS)) {
+          fail(ST_TIMEOUT_MMA);
+          goto done;
+        }
+        umma::fence_after_sync();
+        const uint32_t d = tmem + (uint32_t)(acc * a.cout);
+        for (int grp = 0; grp < 9; ++grp) {
+          const int s = it_a & 1;
+          if (!mbar_wait_bounded(&full_a[s], (it_a >> 1) & 1, WAIT_NS)) {
+            fail(ST_TIMEOUT_MMA);
+            goto done;
+          }
+          umma::fence_after_sync();
+          const uint32_t abase = smem_u32(sa + (size_t)s * a_bytes);
+          for (int dx = 0; dx < 3; ++dx) {
+            const int sbi = it_b % nb;
+            if (!mbar_wait_bounded(&full_b[sbi], (it_b / nb) & 1, WAIT_NS)) {
+              fail(ST_TIMEOUT_MMA);
+              goto done;
+            }
+            umma::fence_after_sync();
+            const uint32_t bbase = smem_u32(sb + (size_t)sbi * b_bytes);
+            for (int kc = 0; kc < a.cin / 16; ++kc) {
+              const uint64_t ad = umma::smem_desc(abase + dx * 16 + 2 * kc * SLAB_PITCH, SLAB_PITCH, 128);
+              const uint64_t bd = umma::smem_desc(bbase + 2 * kc * b_lbo, b_lbo, 128);
+              umma::mma_bf16(d, ad, bd, idesc, (grp | dx | kc) != 0);
+            }
+            umma::commit(&empty_b[sbi]);
+            ++it_b;
+          }
+          umma::commit(&empty_a[s]);
+          ++it_a;
+        }
+        umma::commit(&acc_full[acc]);
+      }
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31, one output row per thread
+    const int q = warp & 3;
+    const int r = 32 * q + lane;
+    int t_local = 0;
+    for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++t_local) {
+      const int acc = t_local & 1;
+      if (!mbar_wait_bounded(&acc_full[acc], (t_local >> 1) & 1, WAIT_NS)) {
+        fail(ST_TIMEOUT_EPI);
+        goto done;
+      }
+      umma::fence_after_sync();
+      const long long p = (long long)tile * TILE_M + r;
+      const bool in = interior(g, p);
+      const long long roff = (g.margin + p) * 16;
+      for (int c0 = 0; c0 < a.cout; c0 += 16) {
+        float v[16];
+        umma::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * a.cout + c0), v);
+        if (a.bias) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] += __ldg(a.bias + c0 + j);
+        }
+        if (a.flags & PVD_UNET_ACT_LEAKY) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = v[j] > 0.f ? v[j] : v[j] * a.slope;
+        }
+        const int pl = c0 >> 3;
+        if (in && a.mask) {
+          float m[16];
+          unpack8(*reinterpret_cast<const uint4*>(a.mask + pl * a.plane + roff), m);
+          unpack8(*reinterpret_cast<const uint4*>(a.mask + (pl + 1) * a.plane + roff), m + 8);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] *= leaky_grad(m[j], a.slope);
+        }
+        if (in && (a.flags & PVD_UNET_ACCUMULATE)) {
+          float o[16];
+          unpack8(*reinterpret_cast<const uint4*>(a.y + pl * a.plane + roff), o);
+          unpack8(*reinterpret_cast<const uint4*>(a.y + (pl + 1) * a.plane + roff), o + 8);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] += o[j];
+        }
+        if (!in) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = 0.f;
+        }
+        *reinterpret_cast<uint4*>(a.y + pl * a.plane + roff) = pack8(v);
+        *reinterpret_cast<uint4*>(a.y + (pl + 1) * a.plane + roff) = pack8(v + 8);
+      }
+      umma::fence_before_sync();
+      umma::mbar_arrive(&acc_empty[acc]);
+    }
+  }
+done:
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, ncols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// weight gradient: partial[split][mt][m][n] = sum over this split's rows
+// ---------------------------------------------------------------------------
+struct WgradArgs {
+  const uint8_t* x;  // input planes (cin channels)
+  const uint8_t* g;  // output-gradient planes (cout channels)
+  float* partial;
+  int cin, cout, m_tiles, splits, ns;
+  long long rows_per_split, plane;
+  Geo geo;
+};
+
+__global__ void __launch_bounds__(CONV_THREADS, 1) k_wgrad(const WgradArgs a) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  const uint32_t plane_tile = WG_KT * 16;  // bytes of one 8-channel group of a stage
+  const uint32_t a_bytes = 16 * plane_tile;
+  const uint32_t b_bytes = (uint32_t)(a.cout / 8) * plane_tile;
+  const uint32_t st_bytes = a_bytes + b_bytes;
+  const int ns = a.ns;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sm + (size_t)ns * st_bytes);
+  uint64_t* empty = full + ns;
+  uint64_t* acc_full = empty + ns;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(acc_full + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x, split = blockIdx.y;
+  const uint32_t ncols = umma::tmem_cols(a.cout);
+  const Geo& g = a.geo;
+  const long long k_begin = (long long)split * a.rows_per_split;
+  const long long k_end = min(g.np_tiles, k_begin + a.rows_per_split);
+  const int n_st = k_end > k_begin ? (int)((k_end - k_begin) / WG_KT) : 0;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < ns; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(acc_full, 1);
+    fence_mbar_init();
+  }
+  if (warp == 1) umma::tmem_alloc(tslot, ncols);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // source rows of the 16 A groups (tap, 8-channel chunk) of this M tile
+      long long a_off[16];
+      int a_pl[16];
+      for (int grp = 0; grp < 16; ++grp) {
+        const int mg = mt * 128 + grp * 8;
+        int tap = mg / a.cin, ch = (mg % a.cin) / 8;
+        if (tap >= 27) tap = 0, ch = 0;  // rows beyond 27 x cin: loaded but never stored
+        a_off[grp] = tap_offset(g, tap);
+        a_pl[grp] = ch;
+      }
+      for (int st = 0; st < n_st; ++st) {
+        const int s = st % ns;
+        if (!mbar_wait_bounded(&empty[s], ((st / ns) & 1) ^ 1, WAIT_NS)) {
+          fail(ST_TIMEOUT_LOAD);
+          goto done;
+        }
+        mbar_arrive_expect_tx(&full[s], st_bytes);
+        const long long k0 = k_begin + (long long)st * WG_KT;
+        uint8_t* dst = sm + (size_t)s * st_bytes;
+        for (int grp = 0; grp < 16; ++grp)
+          umma::bulk_g2s(dst + grp * plane_tile, a.x + a_pl[grp] * a.plane + (g.margin + k0 + a_off[grp]) * 16,
+                         plane_tile, &full[s]);
+        for (int c = 0; c < a.cout / 8; ++c)
+          umma::bulk_g2s(dst + a_bytes + c * plane_tile, a.g + c * a.plane + (g.margin + k0) * 16, plane_tile,
+                         &full[s]);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = umma::idesc_bf16(a.cout, true, true);
+      for (int st = 0; st < n_st; ++st) {
+        const int s = st % ns;
+        if (!mbar_wait_bounded(&full[s], (st / ns) & 1, WAIT_NS)) {
+          fail(ST_TIMEOUT_MMA);
+          goto done;
+        }
+        umma::fence_after_sync();
+        const uint32_t base = smem_u32(sm + (size_t)s * st_bytes);
+        for (int j = 0; j < WG_KT / 16; ++j) {
+          const uint64_t ad = umma::smem_desc(base + j * 256, 128, plane_tile);
+          const uint64_t bd = umma::smem_desc(base + a_bytes + j * 256, 128, plane_tile);
+          umma::mma_bf16(tmem, ad, bd, idesc, (st | j) != 0);
+        }
+        umma::commit(&empty[s]);
+      }
+      if (n_st > 0) umma::commit(acc_full);
+    }
+  } else {
+    const int q = warp & 3;
+    const int r = 32 * q + lane;
+    float* out = a.partial + (((size_t)split * a.m_tiles + mt) * 128 + r) * a.cout;
+    if (n_st == 0) {
+      for (int c = 0; c < a.cout; ++c) out[c] = 0.f;
+    } else {
+      if (!mbar_wait_bounded(acc_full, 0, WAIT_NS)) {
+        fail(ST_TIMEOUT_EPI);
+        goto done;
+      }
+      umma::fence_after_sync();
+      for (int c0 = 0; c0 < a.cout; c0 += 16) {
+        float v[16];
+        umma::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+#pragma unroll
+        for (int j = 0; j < 16; j += 4) *reinterpret_cast<float4*>(out + c0 + j) = make_float4(v[j], v[j + 1], v[j + 2], v[j + 3]);
+      }
+    }
+  }
+done:
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, ncols);
+  }
+}
+
+// dw[n][k][tap] = sum over splits of partial[split][mt][m][n], m_global = tap*cin + k = mt*128 + m
+__global__ void k_wgrad_reduce(const float* __restrict__ partial, float* __restrict__ dw, int cin, int cout,
+                               int m_tiles, int splits, int accumulate) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int total = cout * cin * 27;
+  if (i >= total) return;
+  const int tap = i % 27, k = (i / 27) % cin, n = i / (27 * cin);
+  const int mgl = tap * cin + k, mt = mgl / 128, m = mgl % 128;
+  float s = 0.f;
+  for (int sp = 0; sp < splits; ++sp) s += partial[(((size_t)sp * m_tiles + mt) * 128 + m) * cout + n];
+  dw[i] = accumulate ? dw[i] + s : s;
+}
+
+// ---------------------------------------------------------------------------
+// weight packing: FP32 [cout][cin][27] -> BF16 forward [27][cin/8][cout][8] and
+// data-gradient [27][cout/8][cin][8] with the taps mirrored
+// ---------------------------------------------------------------------------
+__global__ void k_pack_weights(const float* __restrict__ w, int cin, int cout, __nv_bfloat16* fwd,
+                               __nv_bfloat16* bwd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cout * cin * 27) return;
+  const int tap = i % 27, k = (i / 27) % cin, n = i / (27 * cin);
+  const __nv_bfloat16 v = __float2bfloat16_rn(w[i]);
+  if (fwd) fwd[(((size_t)tap * (cin / 8) + k / 8) * cout + n) * 8 + (k % 8)] = v;
+  if (bwd) bwd[(((size_t)(26 - tap) * (cout / 8) + n / 8) * cin + k) * 8 + (n % 8)] = v;
+}
+
+// ---------------------------------------------------------------------------
+// memory-bound layers (one thread per voxel and 8-channel plane)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long row_of(const Geo& g, int z, int y, int x) {
+  return g.margin + ((long long)(z + 1) * g.Hp + (y + 1)) * g.Wp + (x + 1);
+}
+
+// network input: channel c of the first n_in volumes (float32, C order, full grid
+// vd x vh x vw) read at origin + voxel, transformed, others zero
+struct InputArgs {
+  const float* vol[4];
+  float scale[4];
+  int mode[4];
+  int n_in, origin[3], vdim[3];
+  uint8_t* x;
+  long long plane;
+  Geo g;
+};
+
+__global__ void k_pack_input(const InputArgs a) {
+  const long long n = (long long)a.g.D * a.g.H * a.g.W;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int x = (int)(i % a.g.W), y = (int)((i / a.g.W) % a.g.H), z = (int)(i / ((long long)a.g.W * a.g.H));
+  const int sz = z + a.origin[0], sy = y + a.origin[1], sx = x + a.origin[2];
+  const bool inside = sz >= 0 && sz < a.vdim[0] && sy >= 0 && sy < a.vdim[1] && sx >= 0 && sx < a.vdim[2];
+  const long long src = inside ? ((long long)sz * a.vdim[1] + sy) * a.vdim[2] + sx : 0;
+  float f[16];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) f[c] = 0.f;
+  for (int c = 0; c < a.n_in; ++c) {
+    float v = inside ? a.vol[c][src] * a.scale[c] : 0.f;
+    if (a.mode[c] == 1) v = sqrtf(fmaxf(v, 0.f));
+    else if (a.mode[c] == 2) v = log1pf(fmaxf(v, 0.f));
+    f[c] = v;
+  }
+  const long long r = row_of(a.g, z, y, x) * 16;
+  *reinterpret_cast<uint4*>(a.x + r) = pack8(f);
+  *reinterpret_cast<uint4*>(a.x + a.plane + r) = pack8(f + 8);
+}
+
+// 2x2x2 average pooling, fine -> coarse
+__global__ void k_pool(const uint8_t* __restrict__ xf, Geo gf, long long plane_f, uint8_t* yc, Geo gc,
+                       long long plane_c, int c8) {
+  const long long n = (long long)gc.D * gc.H * gc.W * c8;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int pl = (int)(i % c8);
+  const long long v = i / c8;
+  const int x = (int)(v % gc.W), y = (int)((v / gc.W) % gc.H), z = (int)(v / ((long long)gc.W * gc.H));
+  float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int d = 0; d < 8; ++d) {
+    float f[8];
+    unpack8(*reinterpret_cast<const uint4*>(xf + pl * plane_f +
+                                            row_of(gf, 2 * z + (d >> 2), 2 * y + ((d >> 1) & 1), 2 * x + (d & 1)) * 16),
+            f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s[j] += f[j];
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s[j] *= 0.125f;
+  *reinterpret_cast<uint4*>(yc + pl * plane_c + row_of(gc, z, y, x) * 16) = pack8(s);
+}
+
+// pooling backward: dxf = ((accumulate ? dxf : 0) + dyc[parent] / 8) * leaky'(mask)
+__global__ void k_pool_bwd(const uint8_t* __restrict__ dyc, Geo gc, long long plane_c, uint8_t* dxf,
+                           const uint8_t* __restrict__ mask, Geo gf, long long plane_f, int c8, int accumulate,
+                           float slope) {
+  const long long n = (long long)gf.D * gf.H * gf.W * c8;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int pl = (int)(i % c8);
+  const long long v = i / c8;
+  const int x = (int)(v % gf.W), y = (int)((v / gf.W) % gf.H), z = (int)(v / ((long long)gf.W * gf.H));
+  float d[8], o[8];
+  unpack8(*reinterpret_cast<const uint4*>(dyc + pl * plane_c + row_of(gc, z >> 1, y >> 1, x >> 1) * 16), d);
+  const long long r = pl * plane_f + row_of(gf, z, y, x) * 16;
+  if (accumulate) unpack8(*reinterpret_cast<const uint4*>(dxf + r), o);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) d[j] = d[j] * 0.125f + (accumulate ? o[j] : 0.f);
+  if (mask) {
+    float m[8];
+    unpack8(*reinterpret_cast<const uint4*>(mask + r), m);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) d[j] *= leaky_grad(m[j], slope);
+  }
+  *reinterpret_cast<uint4*>(dxf + r) = pack8(d);
+}
+
+// nearest-neighbour 2x upsampling, coarse -> fine
+__global__ void k_upsample(const uint8_t* __restrict__ xc, Geo gc, long long plane_c, uint8_t* yf, Geo gf,
+                           long long plane_f, int c8) {
+  const long long n = (long long)gf.D * gf.H * gf.W * c8;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int pl = (int)(i % c8);
+  const long long v = i / c8;
+  const int x = (int)(v % gf.W), y = (int)((v / gf.W) % gf.H), z = (int)(v / ((long long)gf.W * gf.H));
+  *reinterpret_cast<uint4*>(yf + pl * plane_f + row_of(gf, z, y, x) * 16) =
+      *reinterpret_cast<const uint4*>(xc + pl * plane_c + row_of(gc, z >> 1, y >> 1, x >> 1) * 16);
+}
+
+// upsampling backward: dxc = sum of the 8 children's dyf, times leaky'(mask)
+__global__ void k_upsample_bwd(const uint8_t* __restrict__ dyf, Geo gf, long long plane_f, uint8_t* dxc,
+                               const uint8_t* __restrict__ mask, Geo gc, long long plane_c, int c8, float slope) {
+  const long long n = (long long)gc.D * gc.H * gc.W * c8;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int pl = (int)(i % c8);
+  const long long v = i / c8;
+  const int x = (int)(v % gc.W), y = (int)((v / gc.W) % gc.H), z = (int)(v / ((long long)gc.W * gc.H));
+  float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int d = 0; d < 8; ++d) {
+    float f[8];
+    unpack8(*reinterpret_cast<const uint4*>(dyf + pl * plane_f +
+                                            row_of(gf, 2 * z + (d >> 2), 2 * y + ((d >> 1) & 1), 2 * x + (d & 1)) * 16),
+            f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s[j] += f[j];
+  }
+  const long long r = pl * plane_c + row_of(gc, z, y, x) * 16;
+  if (mask) {
+    float m[8];
+    unpack8(*reinterpret_cast<const uint4*>(mask + r), m);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s[j] *= leaky_grad(m[j], slope);
+  }
+  *reinterpret_cast<uint4*>(dxc + r) = pack8(s);
+}
+
+// head: out[k][voxel] = b[k] + sum_c w[k][c] x[voxel][c], k = 0 (log dose ratio), 1 (log squared error)
+__global__ void k_head(const uint8_t* __restrict__ x, long long plane, Geo g, const float* __restrict__ w,
+                       float* __restrict__ out) {
+  const long long n = (long long)g.D * g.H * g.W;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int xx = (int)(i % g.W), y = (int)((i / g.W) % g.H), z = (int)(i / ((long long)g.W * g.H));
+  const long long r = row_of(g, z, y, xx) * 16;
+  float f[16];
+  unpack8(*reinterpret_cast<const uint4*>(x + r), f);
+  unpack8(*reinterpret_cast<const uint4*>(x + plane + r), f + 8);
+  float o0 = w[32], o1 = w[33];
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    o0 += w[c] * f[c];
+    o1 += w[16 + c] * f[c];
+  }
+  out[i] = o0;
+  out[n + i] = o1;
+}
+
+// loss and head backward.  pred: [2][n] from k_head; target/weight: full volumes
+// read at origin.  Per voxel e = mu - t, l = log(e^2 + eps):
+//   loss0 = sum w e^2 / n,  loss1 = sum w (s - l)^2 / n  (l taken as constant)
+// gx (16-channel planes) = (g_mu w0 + g_s w1) * leaky'(x); per-block partial sums
+// of [dw0(16) dw1(16) db0 db1 loss0 loss1] go to part[block][36].
+constexpr int HEAD_THREADS = 256;
+__global__ void __launch_bounds__(HEAD_THREADS) k_head_loss(const uint8_t* __restrict__ x, long long plane, Geo g,
+                                                           const float* __restrict__ w, const float* __restrict__ pred,
+                                                           const float* __restrict__ target,
+                                                           const float* __restrict__ weight, int o0, int o1, int o2,
+                                                           int vd, int vh, int vw, float inv_n, float eps, float slope,
+                                                           uint8_t* gx, float* __restrict__ part) {
+  __shared__ float red[HEAD_THREADS / 32][36];
+  const long long n = (long long)g.D * g.H * g.W;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  float acc[36];
+#pragma unroll
+  for (int j = 0; j < 36; ++j) acc[j] = 0.f;
+  if (i < n) {
+    const int xx = (int)(i % g.W), y = (int)((i / g.W) % g.H), z = (int)(i / ((long long)g.W * g.H));
+    const int sz = z + o0, sy = y + o1, sx = xx + o2;
+    const bool inside = sz >= 0 && sz < vd && sy >= 0 && sy < vh && sx >= 0 && sx < vw;
+    const long long src = inside ? ((long long)sz * vh + sy) * vw + sx : 0;
+    const float t = inside ? target[src] : 0.f, wt = inside ? weight[src] : 0.f;
+    const float mu = pred[i], s = pred[n + i];
+    const float e = mu - t;
+    const float l = logf(e * e + eps);
+    const float gm = 2.f * wt * e * inv_n, gs = 2.f * wt * (s - l) * inv_n;
+    const long long r = row_of(g, z, y, xx) * 16;
+    float f[16], gv[16];
+    unpack8(*reinterpret_cast<const uint4*>(x + r), f);
+    unpack8(*reinterpret_cast<const uint4*>(x + plane + r), f + 8);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      gv[c] = (gm * w[c] + gs * w[16 + c]) * leaky_grad(f[c], slope);
+      acc[c] = gm * f[c];
+      acc[16 + c] = gs * f[c];
+    }
+    acc[32] = gm;
+    acc[33] = gs;
+    acc[34] = wt * e * e * inv_n;
+    acc[35] = wt * (s - l) * (s - l) * inv_n;
+    *reinterpret_cast<uint4*>(gx + r) = pack8(gv);
+    *reinterpret_cast<uint4*>(gx + plane + r) = pack8(gv + 8);
+  }
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < 36; ++j) {
+    float v = acc[j];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wp][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 36) {
+    float v = 0.f;
+    for (int k = 0; k < HEAD_THREADS / 32; ++k) v += red[k][threadIdx.x];
+    part[(size_t)blockIdx.x * 36 + threadIdx.x] = v;
+  }
+}
+
+// sum of per-block rows, fixed order: out[j] = sum_b part[b][j]
+__global__ void k_sum_rows(const float* __restrict__ part, int n_rows, int n_cols, float* __restrict__ out) {
+  const int j = blockIdx.x;
+  float s = 0.f;
+  for (int b = threadIdx.x; b < n_rows; b += blockDim.x) s += part[(size_t)b * n_cols + j];
+  __shared__ float red[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) out[j] = v;
+  }
+}
+
+// bias gradient partials: part[block][c] = sum over this block's interior voxels of G[voxel][c]
+constexpr int BIAS_VOX = 256;
+__global__ void k_bias_grad(const uint8_t* __restrict__ gt, long long plane, Geo g, int c8, float* __restrict__ part) {
+  // block: 256 voxels x all planes; thread t handles voxel t for each plane
+  const long long n = (long long)g.D * g.H * g.W;
+  const long long i = (long long)blockIdx.x * BIAS_VOX + threadIdx.x;
+  __shared__ float red[BIAS_VOX / 32][8];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  long long r = -1;
+  if (i < n) {
+    const int xx = (int)(i % g.W), y = (int)((i / g.W) % g.H), z = (int)(i / ((long long)g.W * g.H));
+    r = row_of(g, z, y, xx) * 16;
+  }
+  for (int pl = 0; pl < c8; ++pl) {
+    float f[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (r >= 0) unpack8(*reinterpret_cast<const uint4*>(gt + pl * plane + r), f);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float v = f[j];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[wp][j] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+      float v = 0.f;
+      for (int k = 0; k < BIAS_VOX / 32; ++k) v += red[k][threadIdx.x];
+      part[(size_t)blockIdx.x * (c8 * 8) + pl * 8 + threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// corrected dose on the volume voxels the crop covers: dose_conv * exp(clamp(mu)),
+// or dose_conv itself where the predicted error sqrt(exp(s)) exceeds sigma_max
+__global__ void k_apply(const float* __restrict__ pred, Geo g, const float* __restrict__ dose, int o0, int o1, int o2,
+                        int vd, int vh, int vw, float sigma_max, float mu_clamp, float* __restrict__ out,
+                        uint8_t* __restrict__ fallback) {
+  const long long n = (long long)g.D * g.H * g.W;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int xx = (int)(i % g.W), y = (int)((i / g.W) % g.H), z = (int)(i / ((long long)g.W * g.H));
+  const int sz = z + o0, sy = y + o1, sx = xx + o2;
+  if (sz < 0 || sz >= vd || sy < 0 || sy >= vh || sx < 0 || sx >= vw) return;
+  const long long v = ((long long)sz * vh + sy) * vw + sx;
+  const float mu = fminf(fmaxf(pred[i], -mu_clamp), mu_clamp);
+  const bool fb = !(expf(0.5f * pred[n + i]) <= sigma_max);
+  out[v] = fb ? dose[v] : dose[v] * expf(mu);
+  if (fallback) fallback[v] = fb ? 1 : 0;
+}
+
+// Adam with decoupled weight decay on FP32 parameters
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m,
+                       float* __restrict__ v, long long n, float lr, float b1, float b2, float eps, float wd,
+                       float c1, float c2) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gg = gr[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gg;
+  const float vi = b2 * v[i] + (1.f - b2) * gg * gg;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * ((mi / c1) / (sqrtf(vi / c2) + eps) + wd * p[i]);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static int g_sms = 0;
+static int sm_count() {
+  if (g_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms <= 0) g_sms = 1;
+  }
+  return g_sms;
+}
+
+static bool ch_ok(int c) { return c >= 16 && c <= 256 && c % 16 == 0; }
+static bool al16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
+static size_t conv_smem(int cin, int cout, int nb) {
+  return 2 * (size_t)(cin / 8) * SLAB_PITCH + (size_t)nb * cin * cout * 2 + (size_t)(8 + 2 * nb) * 8 + 16;
+}
+
+static pvd_status geo_check(const pvd_unet_geom* g) {
+  if (!g) return set_error(PVD_ERR_ARG, "unet: null geometry");
+  pvd_unet_geom ref;
+  if (pvd_unet_geometry(g->dims[0], g->dims[1], g->dims[2], &ref) != PVD_OK) return PVD_ERR_ARG;
+  if (ref.rows != g->rows || ref.margin != g->margin || ref.padded != g->padded || ref.padded_tiles != g->padded_tiles)
+    return set_error(PVD_ERR_ARG, "unet: geometry not produced by pvd_unet_geometry");
+  return PVD_OK;
+}
+
+static unsigned blocks_for(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace unet
+}  // namespace pvd
+
+using namespace pvd;
+using namespace pvd::unet;
+
+extern "C" pvd_status pvd_unet_geometry(int d, int h, int w, pvd_unet_geom* out) {
+  if (!out) return set_error(PVD_ERR_ARG, "pvd_unet_geometry: null output");
+  if (d < 1 || h < 1 || w < 1 || d > 4096 || h > 4096 || w > 4096)
+    return set_error(PVD_ERR_ARG, "pvd_unet_geometry: dims must be in [1, 4096]");
+  const long long hp = h + 2, wp = w + 2, dp = d + 2;
+  out->dims[0] = d;
+  out->dims[1] = h;
+  out->dims[2] = w;
+  out->padded = dp * hp * wp;
+  out->padded_tiles = (out->padded + TILE_M - 1) / TILE_M * TILE_M;
+  out->margin = (hp * wp + wp + 2 + 7) / 8 * 8;
+  out->rows = out->margin + out->padded_tiles + out->margin;
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_conv3d(const pvd_unet_geom* geom, const void* x, int cin, const void* w_packed,
+                                      const float* bias, void* y, int cout, const void* mask, int flags, float slope,
+                                      pvd_stream stream) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!ch_ok(cin) || !ch_ok(cout)) return set_error(PVD_ERR_ARG, "pvd_unet_conv3d: channels must be multiples of 16 in [16, 256]");
+  if (!x || !w_packed || !y || !al16(x) || !al16(w_packed) || !al16(y) || (mask && !al16(mask)))
+    return set_error(PVD_ERR_ARG, "pvd_unet_conv3d: tensors must be non-null and 16-byte aligned");
+  if (flags & ~(PVD_UNET_ACT_LEAKY | PVD_UNET_ACCUMULATE)) return set_error(PVD_ERR_ARG, "pvd_unet_conv3d: unknown flags");
+  int nb = 4;
+  while (nb > 2 && conv_smem(cin, cout, nb) > (size_t)MAX_SMEM) --nb;
+  const size_t smem = conv_smem(cin, cout, nb);
+  if (smem > (size_t)MAX_SMEM) return set_error(PVD_ERR_UNSUPPORTED, "pvd_unet_conv3d: channel counts need more shared memory than a CTA has");
+  ConvArgs a;
+  a.x = (const uint8_t*)x;
+  a.w = (const uint8_t*)w_packed;
+  a.bias = bias;
+  a.y = (uint8_t*)y;
+  a.mask = (const uint8_t*)mask;
+  a.cin = cin;
+  a.cout = cout;
+  a.flags = flags;
+  a.nb = nb;
+  a.slope = slope;
+  a.g = make_geo(geom);
+  a.plane = a.g.rows * 16;
+  a.n_tiles = (int)(a.g.np_tiles / TILE_M);
+  PVD_CUDA_TRY(cudaFuncSetAttribute(k_conv3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 1;
+  PVD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv3, CONV_THREADS, smem));
+  const int by_tmem = (int)(512 / umma::tmem_cols(2 * cout));
+  occ = std::max(1, std::min(occ, by_tmem));
+  const int grid = std::min(a.n_tiles, sm_count() * occ);
+  k_conv3<<<grid, CONV_THREADS, smem, (cudaStream_t)stream>>>(a);
+  PVD_LAUNCH_CHECK("k_conv3");
+  return PVD_OK;
+}
+
+static void wgrad_plan(const Geo& g, int cin, int cout, int* m_tiles, int* splits, long long* per, int* ns) {
+  *m_tiles = (27 * cin + 127) / 128;
+  const long long n_k = g.np_tiles / WG_KT;
+  long long want = std::max<long long>(1, (2LL * sm_count() + *m_tiles - 1) / *m_tiles);
+  want = std::min(want, n_k);
+  const long long per_k = (n_k + want - 1) / want;
+  *per = per_k * WG_KT;
+  *splits = (int)((n_k + per_k - 1) / per_k);
+  const size_t st_bytes = 16 * WG_KT * 16 + (size_t)(cout / 8) * WG_KT * 16;
+  int s = 6;
+  while (s > 2 && (size_t)s * st_bytes + (2 * s + 1) * 8 + 16 > (size_t)MAX_SMEM) --s;
+  *ns = s;
+}
+
+extern "C" pvd_status pvd_unet_wgrad_workspace(const pvd_unet_geom* geom, int cin, int cout, size_t* bytes) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!bytes || !ch_ok(cin) || !ch_ok(cout)) return set_error(PVD_ERR_ARG, "pvd_unet_wgrad_workspace: bad arguments");
+  int mt, sp, ns;
+  long long per;
+  wgrad_plan(make_geo(geom), cin, cout, &mt, &sp, &per, &ns);
+  *bytes = (size_t)sp * mt * 128 * cout * sizeof(float);
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_conv3d_wgrad(const pvd_unet_geom* geom, const void* x, int cin, const void* grad,
+                                            int cout, float* dw, int accumulate, void* workspace,
+                                            size_t workspace_bytes, pvd_stream stream) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!ch_ok(cin) || !ch_ok(cout)) return set_error(PVD_ERR_ARG, "pvd_unet_conv3d_wgrad: channels must be multiples of 16 in [16, 256]");
+  if (!x || !grad || !dw || !workspace || !al16(x) || !al16(grad) || !al16(workspace))
+    return set_error(PVD_ERR_ARG, "pvd_unet_conv3d_wgrad: tensors must be non-null and 16-byte aligned");
+  WgradArgs a;
+  a.geo = make_geo(geom);
+  wgrad_plan(a.geo, cin, cout, &a.m_tiles, &a.splits, &a.rows_per_split, &a.ns);
+  const size_t need = (size_t)a.splits * a.m_tiles * 128 * cout * sizeof(float);
+  if (workspace_bytes < need) return set_error(PVD_ERR_ARG, "pvd_unet_conv3d_wgrad: workspace smaller than pvd_unet_wgrad_workspace");
+  a.x = (const uint8_t*)x;
+  a.g = (const uint8_t*)grad;
+  a.partial = (float*)workspace;
+  a.cin = cin;
+  a.cout = cout;
+  a.plane = a.geo.rows * 16;
+  const size_t st_bytes = 16 * WG_KT * 16 + (size_t)(cout / 8) * WG_KT * 16;
+  const size_t smem = (size_t)a.ns * st_bytes + (2 * a.ns + 1) * 8 + 16;
+  PVD_CUDA_TRY(cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_wgrad<<<dim3(a.m_tiles, a.splits), CONV_THREADS, smem, (cudaStream_t)stream>>>(a);
+  PVD_LAUNCH_CHECK("k_wgrad");
+  const int total = cout * cin * 27;
+  k_wgrad_reduce<<<blocks_for(total, 256), 256, 0, (cudaStream_t)stream>>>(a.partial, dw, cin, cout, a.m_tiles,
+                                                                          a.splits, accumulate);
+  PVD_LAUNCH_CHECK("k_wgrad_reduce");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_pack_weights(const float* w, int cin, int cout, void* fwd_packed, void* bwd_packed,
+                                            pvd_stream stream) {
+  if (!w || (!fwd_packed && !bwd_packed) || !ch_ok(cin) || !ch_ok(cout))
+    return set_error(PVD_ERR_ARG, "pvd_unet_pack_weights: bad arguments");
+  const int total = cout * cin * 27;
+  k_pack_weights<<<blocks_for(total, 256), 256, 0, (cudaStream_t)stream>>>(w, cin, cout, (__nv_bfloat16*)fwd_packed,
+                                                                          (__nv_bfloat16*)bwd_packed);
+  PVD_LAUNCH_CHECK("k_pack_weights");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_pack_input(const pvd_unet_geom* geom, const float* const* volumes, const float* scales,
+                                          const int* modes, int n_in, const int* vol_dims, const int* origin, void* x,
+                                          pvd_stream stream) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (n_in < 1 || n_in > 4 || !volumes || !scales || !modes || !vol_dims || !origin || !x || !al16(x))
+    return set_error(PVD_ERR_ARG, "pvd_unet_pack_input: bad arguments");
+  InputArgs a;
+  a.g = make_geo(geom);
+  for (int i = 0; i < 3; ++i) {
+    a.origin[i] = origin[i];
+    a.vdim[i] = vol_dims[i];
+    if (vol_dims[i] < 1) return set_error(PVD_ERR_ARG, "pvd_unet_pack_input: bad volume dims");
+  }
+  for (int c = 0; c < 4; ++c) {
+    a.vol[c] = c < n_in ? volumes[c] : nullptr;
+    a.scale[c] = c < n_in ? scales[c] : 0.f;
+    a.mode[c] = c < n_in ? modes[c] : 0;
+    if (c < n_in && (!volumes[c] || modes[c] < 0 || modes[c] > 2))
+      return set_error(PVD_ERR_ARG, "pvd_unet_pack_input: null volume or unknown mode");
+  }
+  a.n_in = n_in;
+  a.x = (uint8_t*)x;
+  a.plane = a.g.rows * 16;
+  const long long n = (long long)a.g.D * a.g.H * a.g.W;
+  k_pack_input<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(a);
+  PVD_LAUNCH_CHECK("k_pack_input");
+  return PVD_OK;
+}
+
+static pvd_status pair_check(const pvd_unet_geom* fine, const pvd_unet_geom* coarse, int c, const void* p, const void* q,
+                             const char* who) {
+  pvd_status st = geo_check(fine);
+  if (st != PVD_OK) return st;
+  st = geo_check(coarse);
+  if (st != PVD_OK) return st;
+  for (int i = 0; i < 3; ++i)
+    if (fine->dims[i] != 2 * coarse->dims[i]) return set_error(PVD_ERR_ARG, std::string(who) + ": fine dims must be twice the coarse dims");
+  if (c < 8 || c % 8 || !p || !q || !al16(p) || !al16(q))
+    return set_error(PVD_ERR_ARG, std::string(who) + ": bad channel count or tensor");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_pool(const pvd_unet_geom* fine, const void* x, const pvd_unet_geom* coarse, void* y,
+                                    int channels, pvd_stream stream) {
+  pvd_status st = pair_check(fine, coarse, channels, x, y, "pvd_unet_pool");
+  if (st != PVD_OK) return st;
+  const Geo gf = make_geo(fine), gc = make_geo(coarse);
+  const long long n = (long long)gc.D * gc.H * gc.W * (channels / 8);
+  k_pool<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>((const uint8_t*)x, gf, gf.rows * 16, (uint8_t*)y, gc,
+                                                              gc.rows * 16, channels / 8);
+  PVD_LAUNCH_CHECK("k_pool");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_pool_backward(const pvd_unet_geom* coarse, const void* dy, const pvd_unet_geom* fine,
+                                             void* dx, const void* mask, int channels, int accumulate, float slope,
+                                             pvd_stream stream) {
+  pvd_status st = pair_check(fine, coarse, channels, dy, dx, "pvd_unet_pool_backward");
+  if (st != PVD_OK) return st;
+  const Geo gf = make_geo(fine), gc = make_geo(coarse);
+  const long long n = (long long)gf.D * gf.H * gf.W * (channels / 8);
+  k_pool_bwd<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>((const uint8_t*)dy, gc, gc.rows * 16, (uint8_t*)dx,
+                                                                  (const uint8_t*)mask, gf, gf.rows * 16,
+                                                                  channels / 8, accumulate, slope);
+  PVD_LAUNCH_CHECK("k_pool_bwd");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_upsample(const pvd_unet_geom* coarse, const void* x, const pvd_unet_geom* fine, void* y,
+                                        int channels, pvd_stream stream) {
+  pvd_status st = pair_check(fine, coarse, channels, x, y, "pvd_unet_upsample");
+  if (st != PVD_OK) return st;
+  const Geo gf = make_geo(fine), gc = make_geo(coarse);
+  const long long n = (long long)gf.D * gf.H * gf.W * (channels / 8);
+  k_upsample<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>((const uint8_t*)x, gc, gc.rows * 16, (uint8_t*)y,
+                                                                  gf, gf.rows * 16, channels / 8);
+  PVD_LAUNCH_CHECK("k_upsample");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_upsample_backward(const pvd_unet_geom* fine, const void* dy, const pvd_unet_geom* coarse,
+                                                 void* dx, const void* mask, int channels, float slope,
+                                                 pvd_stream stream) {
+  pvd_status st = pair_check(fine, coarse, channels, dy, dx, "pvd_unet_upsample_backward");
+  if (st != PVD_OK) return st;
+  const Geo gf = make_geo(fine), gc = make_geo(coarse);
+  const long long n = (long long)gc.D * gc.H * gc.W * (channels / 8);
+  k_upsample_bwd<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>((const uint8_t*)dy, gf, gf.rows * 16,
+                                                                      (uint8_t*)dx, (const uint8_t*)mask, gc,
+                                                                      gc.rows * 16, channels / 8, slope);
+  PVD_LAUNCH_CHECK("k_upsample_bwd");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_head(const pvd_unet_geom* geom, const void* x, const float* w_head, float* out,
+                                    pvd_stream stream) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!x || !w_head || !out || !al16(x)) return set_error(PVD_ERR_ARG, "pvd_unet_head: bad arguments");
+  const Geo g = make_geo(geom);
+  const long long n = (long long)g.D * g.H * g.W;
+  k_head<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>((const uint8_t*)x, g.rows * 16, g, w_head, out);
+  PVD_LAUNCH_CHECK("k_head");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_head_loss_workspace(const pvd_unet_geom* geom, size_t* bytes) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!bytes) return set_error(PVD_ERR_ARG, "pvd_unet_head_loss_workspace: null output");
+  const long long n = (long long)geom->dims[0] * geom->dims[1] * geom->dims[2];
+  *bytes = (size_t)blocks_for(n, HEAD_THREADS) * 36 * sizeof(float);
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_head_loss(const pvd_unet_geom* geom, const void* x, const float* w_head,
+                                         const float* pred, const float* target, const float* weight,
+                                         const int* vol_dims, const int* origin, float eps, float slope, void* grad_x,
+                                         float* grads_and_loss, void* workspace, size_t workspace_bytes,
+                                         pvd_stream stream) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!x || !w_head || !pred || !target || !weight || !vol_dims || !origin || !grad_x || !grads_and_loss ||
+      !workspace || !al16(x) || !al16(grad_x))
+    return set_error(PVD_ERR_ARG, "pvd_unet_head_loss: bad arguments");
+  for (int i = 0; i < 3; ++i)
+    if (vol_dims[i] < 1) return set_error(PVD_ERR_ARG, "pvd_unet_head_loss: bad volume dims");
+  const Geo g = make_geo(geom);
+  const long long n = (long long)g.D * g.H * g.W;
+  const unsigned nblk = blocks_for(n, HEAD_THREADS);
+  if (workspace_bytes < (size_t)nblk * 36 * sizeof(float))
+    return set_error(PVD_ERR_ARG, "pvd_unet_head_loss: workspace smaller than pvd_unet_head_loss_workspace");
+  k_head_loss<<<nblk, HEAD_THREADS, 0, (cudaStream_t)stream>>>(
+      (const uint8_t*)x, g.rows * 16, g, w_head, pred, target, weight, origin[0], origin[1], origin[2], vol_dims[0],
+      vol_dims[1], vol_dims[2], (float)(1.0 / (double)n), eps, slope, (uint8_t*)grad_x, (float*)workspace);
+  PVD_LAUNCH_CHECK("k_head_loss");
+  k_sum_rows<<<36, 256, 0, (cudaStream_t)stream>>>((const float*)workspace, (int)nblk, 36, grads_and_loss);
+  PVD_LAUNCH_CHECK("k_sum_rows");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_bias_grad_workspace(const pvd_unet_geom* geom, int channels, size_t* bytes) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!bytes || channels < 8 || channels % 8) return set_error(PVD_ERR_ARG, "pvd_unet_bias_grad_workspace: bad arguments");
+  const long long n = (long long)geom->dims[0] * geom->dims[1] * geom->dims[2];
+  *bytes = (size_t)blocks_for(n, BIAS_VOX) * channels * sizeof(float);
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_bias_grad(const pvd_unet_geom* geom, const void* grad, int channels, float* db,
+                                         void* workspace, size_t workspace_bytes, pvd_stream stream) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!grad || !db || !workspace || channels < 8 || channels % 8 || !al16(grad))
+    return set_error(PVD_ERR_ARG, "pvd_unet_bias_grad: bad arguments");
+  const Geo g = make_geo(geom);
+  const long long n = (long long)g.D * g.H * g.W;
+  const unsigned nblk = blocks_for(n, BIAS_VOX);
+  if (workspace_bytes < (size_t)nblk * channels * sizeof(float))
+    return set_error(PVD_ERR_ARG, "pvd_unet_bias_grad: workspace smaller than pvd_unet_bias_grad_workspace");
+  k_bias_grad<<<nblk, BIAS_VOX, 0, (cudaStream_t)stream>>>((const uint8_t*)grad, g.rows * 16, g, channels / 8,
+                                                          (float*)workspace);
+  PVD_LAUNCH_CHECK("k_bias_grad");
+  k_sum_rows<<<channels, 256, 0, (cudaStream_t)stream>>>((const float*)workspace, (int)nblk, channels, db);
+  PVD_LAUNCH_CHECK("k_sum_rows");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_apply_correction(const pvd_unet_geom* geom, const float* pred, const float* dose_conv,
+                                                const int* vol_dims, const int* origin, float sigma_max,
+                                                float mu_clamp, float* dose_out, uint8_t* fallback,
+                                                pvd_stream stream) {
+  pvd_status st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!pred || !dose_conv || !vol_dims || !origin || !dose_out || !(mu_clamp > 0.f))
+    return set_error(PVD_ERR_ARG, "pvd_unet_apply_correction: bad arguments");
+  for (int i = 0; i < 3; ++i)
+    if (vol_dims[i] < 1) return set_error(PVD_ERR_ARG, "pvd_unet_apply_correction: bad volume dims");
+  const Geo g = make_geo(geom);
+  const long long n = (long long)g.D * g.H * g.W;
+  k_apply<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(pred, g, dose_conv, origin[0], origin[1], origin[2],
+                                                               vol_dims[0], vol_dims[1], vol_dims[2], sigma_max,
+                                                               mu_clamp, dose_out, fallback);
+  PVD_LAUNCH_CHECK("k_apply");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_adam_step(float* params, const float* grads, float* m, float* v, int64_t n, float lr,
+                                    float beta1, float beta2, float eps, float weight_decay, int step,
+                                    pvd_stream stream) {
+  if (!params || !grads || !m || !v || n < 0 || step < 1) return set_error(PVD_ERR_ARG, "pvd_adam_step: bad arguments");
+  if (n == 0) return PVD_OK;
+  const float c1 = (float)(1.0 - std::pow((double)beta1, step));
+  const float c2 = (float)(1.0 - std::pow((double)beta2, step));
+  k_adam<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(params, grads, m, v, n, lr, beta1, beta2, eps,
+                                                              weight_decay, c1, c2);
+  PVD_LAUNCH_CHECK("k_adam");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_status(int* code, int reset) {
+  if (!code) return set_error(PVD_ERR_ARG, "pvd_unet_status: null output");
+  PVD_CUDA_TRY(cudaMemcpyFromSymbol(code, g_unet_status, sizeof(int)));
+  if (reset) {
+    const int z = 0;
+    PVD_CUDA_TRY(cudaMemcpyToSymbol(g_unet_status, &z, sizeof(int)));
+  }
+  if (*code != 0) return set_error(PVD_ERR_TIMEOUT, "unet: a bounded tensor-core pipeline wait ran out (code " + std::to_string(*code) + ")");
+  return PVD_OK;
+}

@@ -1,0 +1,96 @@
+"""Learned-correction network: CPU checks (no GPU needed).
+
+* the oracle's hand-written backward equals torch autograd (float64, no rounding);
+* the product's layer table equals the oracle's;
+* the U-Net entry points reject bad geometry, channel counts and pointers
+  before any CUDA call.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import unet as ou
+from pyvoxeldosimetry_gb300 import _native as N
+from pyvoxeldosimetry_gb300.core import learned_correction as lc
+
+
+def _random_problem(dims=(16, 16, 16), seed=0):
+    rng = np.random.default_rng(seed)
+    flat = np.zeros(ou.n_params())
+    o = 0
+    for _, ci, co in ou.LAYERS:
+        flat[o:o + co * ci * 27] = rng.normal(0, np.sqrt(2.0 / (27 * ci)), co * ci * 27)
+        o += co * ci * 27
+        flat[o:o + co] = rng.normal(0, 0.05, co)
+        o += co
+    flat[o:o + 34] = rng.normal(0, 0.3, 34)
+    vols = [rng.random(dims).astype(np.float32) for _ in range(3)]
+    x0 = ou.input_features(vols, [1.0, 1.0, 1.0], [1, 0, 1])
+    target = torch.as_tensor(rng.normal(0, 0.3, dims))
+    weight = torch.as_tensor((rng.random(dims) > 0.3).astype(np.float64))
+    return ou.unpack(flat), x0, target, weight
+
+
+def test_oracle_backward_equals_autograd():
+    params, x0, target, weight = _random_problem()
+    acts = ou.forward(params, x0, bf16=False)
+    g, lm, ls = ou.backward(params, acts, target, weight, bf16=False)
+    ga = ou.autograd_grads(params, x0, target, weight)
+    a, b = ou.flat_grads(g), ou.flat_grads(ga)
+    assert np.linalg.norm(a - b) <= 1e-10 * np.linalg.norm(b)
+    assert lm > 0 and ls > 0
+
+
+def test_layer_tables_agree():
+    assert lc.LAYERS == ou.LAYERS
+    assert lc.HEAD_SIZE == ou.HEAD_SIZE
+    assert lc.SLOPE == ou.SLOPE and lc.EPS == ou.EPS
+    # parameter layout: per layer W [co][ci][27] then b [co], head last
+    n = sum(co * ci * 27 + co for _, ci, co in lc.LAYERS) + lc.HEAD_SIZE
+    assert n == ou.n_params()
+
+
+def test_geometry():
+    g = lc.geometry((16, 12, 10))
+    assert tuple(g.dims) == (16, 12, 10)
+    assert g.padded == 18 * 14 * 12
+    assert g.padded_tiles % 128 == 0 and g.padded_tiles >= g.padded > g.padded_tiles - 128
+    assert g.margin % 8 == 0 and g.margin >= 14 * 12 + 12 + 1
+    assert g.rows == 2 * g.margin + g.padded_tiles
+    lib = N.load()
+    bad = N.UnetGeom()
+    assert lib.pvd_unet_geometry(0, 4, 4, C.byref(bad)) == 1
+
+
+def test_conv_flop_count():
+    # 2 * 27 * sum(ci * co / 8^level) per voxel + the head
+    per = sum(2 * 27 * ci * co / 8 ** lc.LEVEL[n] for n, ci, co in lc.LAYERS) + 64
+    assert lc.conv_flops((8, 8, 8)) == pytest.approx(per * 512)
+
+
+def test_validation_before_any_cuda_call():
+    lib = N.load()
+    g = lc.geometry((8, 8, 8))
+    fake = 1 << 20  # never dereferenced: every case fails validation first
+    # channels not a multiple of 16
+    assert lib.pvd_unet_conv3d(C.byref(g), fake, 24, fake, None, fake, 16, None, 0, 0.01, None) == 1
+    # misaligned tensor
+    assert lib.pvd_unet_conv3d(C.byref(g), fake + 8, 16, fake, None, fake, 16, None, 0, 0.01, None) == 1
+    # unknown flag
+    assert lib.pvd_unet_conv3d(C.byref(g), fake, 16, fake, None, fake, 16, None, 64, 0.01, None) == 1
+    # geometry not from pvd_unet_geometry
+    g2 = lc.geometry((8, 8, 8))
+    g2.rows += 8
+    assert lib.pvd_unet_conv3d(C.byref(g2), fake, 16, fake, None, fake, 16, None, 0, 0.01, None) == 1
+    # workspace too small for the weight gradient
+    sz = C.c_size_t()
+    assert lib.pvd_unet_wgrad_workspace(C.byref(g), 16, 32, C.byref(sz)) == 0 and sz.value > 0
+    assert lib.pvd_unet_conv3d_wgrad(C.byref(g), fake, 16, fake, 32, fake, 0, fake, sz.value - 1, None) == 1
+    # pooling pairs must halve every dim
+    g4 = lc.geometry((4, 4, 2))
+    assert lib.pvd_unet_pool(C.byref(g), fake, C.byref(g4), fake, 16, None) == 1
+    # Adam needs step >= 1
+    assert lib.pvd_adam_step(fake, fake, fake, fake, 10, 1e-3, 0.9, 0.999, 1e-8, 0.0, 0, None) == 1
+    assert "pvd_adam_step" in N.last_error()
