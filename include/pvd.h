@@ -562,7 +562,9 @@ pvd_status pvd_unet_head(const pvd_unet_geom* geom, const void* x, const float* 
  * read at origin (voxels outside them have weight 0).  With e = mu - target and l = log(e^2 + eps):
  *   loss_mu = sum weight e^2 / n,  loss_s = sum weight (s - l)^2 / n
  * (n = D*H*W; l treated as a constant).  Writes grad_x (16-channel tensor: the
- * gradient at the head input times leaky'(x)) and grads_and_loss[36] =
+ * gradient of loss_mu at the head input times leaky'(x); the error head s is
+ * trained on the features without passing its gradient into the network) and
+ * grads_and_loss[36] =
  * [d w_mu (16), d w_s (16), d b_mu, d b_s, loss_mu, loss_s]. */
 pvd_status pvd_unet_head_loss_workspace(const pvd_unet_geom* geom, size_t* bytes);
 pvd_status pvd_unet_head_loss(const pvd_unet_geom* geom, const void* x, const float* w_head, const float* pred,
@@ -577,6 +579,12 @@ pvd_status pvd_unet_head_loss(const pvd_unet_geom* geom, const void* x, const fl
 pvd_status pvd_unet_apply_correction(const pvd_unet_geom* geom, const float* pred, const float* dose_conv,
                                      const int* vol_dims, const int* origin, float sigma_max, float mu_clamp,
                                      float* dose_out, uint8_t* fallback, pvd_stream stream);
+
+/* maxima_d[0] = max activity, maxima_d[1] = max dose over voxels with
+ * density >= rho_min (device float32 volumes of n voxels; non-negative finite
+ * values; 0 if none).  The network input is scaled by their reciprocals. */
+pvd_status pvd_unet_input_maxima(const float* activity, const float* density, const float* dose, int64_t n,
+                                 float rho_min, float* maxima_d, pvd_stream stream);
 
 /* db[c] = sum over interior voxels of grad[v][c] (fixed-order reduction). */
 pvd_status pvd_unet_bias_grad_workspace(const pvd_unet_geom* geom, int channels, size_t* bytes);

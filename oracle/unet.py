@@ -13,6 +13,8 @@ upsampling, skip connections by channel concatenation [upsampled, skip], and a
 predicted log of mu's squared error.  Loss over the n voxels of a crop with
 e = mu - t and l = log(e^2 + eps) (l a constant):
     loss_mu = sum w e^2 / n,   loss_s = sum w (s - l)^2 / n.
+The s head reads the last features without passing its gradient back into the
+network (only loss_mu trains the convolutions).
 
 ``forward`` / ``backward`` restate the GPU computation step by step.  With
 ``bf16=True`` every tensor the GPU stores in BF16 (activations, pooled and
@@ -118,6 +120,7 @@ def forward(params: dict, x0: torch.Tensor, bf16: bool = True) -> dict:
     mu = torch.einsum("c,cdhw->dhw", h[0:16], f) + h[32]
     s = torch.einsum("c,cdhw->dhw", h[16:32], f) + h[33]
     a["pred"] = torch.stack([mu, s])
+    a["s_detached"] = torch.einsum("c,cdhw->dhw", h[16:32], f.detach()) + h[33]
     return a
 
 
@@ -155,7 +158,7 @@ def backward(params: dict, acts: dict, target: torch.Tensor, weight: torch.Tenso
         return r(dx)
 
     A = acts
-    g_d0b = r((h[0:16, None, None, None] * gm + h[16:32, None, None, None] * gs)[None] * _lrelu_grad(A["d0b"]))
+    g_d0b = r((h[0:16, None, None, None] * gm)[None] * _lrelu_grad(A["d0b"]))
     layer("d0b", A["d0a"], g_d0b)
     g_d0a = dgrad("d0b", A["d0a"].shape, g_d0b, A["d0a"])
     layer("d0a", A["cat0"], g_d0a)
@@ -197,7 +200,8 @@ def backward(params: dict, acts: dict, target: torch.Tensor, weight: torch.Tenso
 
 def autograd_grads(params: dict, x0: torch.Tensor, target: torch.Tensor, weight: torch.Tensor):
     """The same network and loss differentiated by torch autograd (float64, no rounding).
-    The log-error target l of the s-loss is detached, as in the hand-written backward."""
+    The log-error target l of the s-loss and the features the s head reads are
+    detached, as in the hand-written backward."""
     leaves = {}
     p2 = {}
     for name, _, _ in LAYERS:
@@ -209,7 +213,7 @@ def autograd_grads(params: dict, x0: torch.Tensor, target: torch.Tensor, weight:
     hd = params["head"].clone().requires_grad_(True)
     p2["head"] = hd
     a = forward(p2, x0, bf16=False)
-    mu, s = a["pred"][0], a["pred"][1]
+    mu, s = a["pred"][0], a["s_detached"]
     n = mu.numel()
     e = mu - target
     l = torch.log(e.detach() ** 2 + EPS)

@@ -17,8 +17,11 @@ from .time_integration.curve_fitting import TimeCurveFitting
 from .core.utils import calculate_dvh, load_dose_map, resample_dose_map, resample_volume, save_dose_map
 from .data.dose_kernels import KernelFactory
 from .batch import BatchDoseCalculator
+from .core.learned_correction import NNCorrectedDoseCalculator, UNet3D
 
 __all__ = [
+    "NNCorrectedDoseCalculator",
+    "UNet3D",
     "DosimetryCalculator",
     "KernelConvolutionCalculator",
     "ActivitySampler",

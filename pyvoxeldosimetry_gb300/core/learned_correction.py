@@ -379,27 +379,36 @@ def input_scales(activity_max: float, dose_max: float) -> Tuple[float, float, fl
     return (1.0 / activity_max if activity_max > 0 else 0.0, 1.0, 1.0 / dose_max if dose_max > 0 else 0.0)
 
 
-def _vol_max(t: torch.Tensor) -> float:
-    st = N.RoiStats()
-    N.check(N.load().pvd_roi_stats(t.data_ptr(), N.PVD_DTYPE_F32, None, 0, t.numel(), C.byref(st),
-                                   _stream_handle(None)))
-    return float(st.max)
+TISSUE_DENSITY = 0.2  # g/cc: lung and denser; dose to air is not a target
+
+
+def _input_scales_device(activity: torch.Tensor, density: torch.Tensor, dose: torch.Tensor):
+    """input_scales from the device maxima of activity and of the dose over tissue."""
+    mx = torch.empty(2, dtype=torch.float32, device=activity.device)
+    N.check(N.load().pvd_unet_input_maxima(activity.data_ptr(), density.data_ptr(), dose.data_ptr(), activity.numel(),
+                                           TISSUE_DENSITY, mx.data_ptr(), _stream_handle(None)))
+    m = mx.cpu()
+    return input_scales(float(m[0]), float(m[1]))
 
 
 def make_pair(activity: np.ndarray, density: np.ndarray, dose_conv: np.ndarray, dose_mc: np.ndarray,
               rel_threshold: float = 0.1, device=None) -> TrainingPair:
     """Target log ratio and weight (host arithmetic on one phantom's doses: data
-    preparation, not the dose path)."""
+    preparation, not the dose path).  Weighted voxels: tissue (density >=
+    TISSUE_DENSITY) whose convolution dose exceeds rel_threshold x its maximum
+    over tissue.  Air is excluded because dose to local mass there is dominated
+    by the 1000x smaller mass, in both methods."""
     dc = np.asarray(dose_conv, np.float64)
     dm = np.asarray(dose_mc, np.float64)
-    thr = rel_threshold * dc.max()
-    ok = (dc > thr) & (dm > 0) & (dc > 0)
+    tissue = np.asarray(density) >= TISSUE_DENSITY
+    thr = rel_threshold * (dc[tissue].max() if tissue.any() else 0.0)
+    ok = tissue & (dc > thr) & (dm > 0) & (dc > 0)
     tgt = np.zeros(dc.shape, np.float32)
     tgt[ok] = np.clip(np.log(dm[ok] / dc[ok]), -3.0, 3.0)
     dev = _require_cuda(device)
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(dev)  # noqa: E731
     return TrainingPair(T(activity), T(density), T(dose_conv), T(dose_mc), T(tgt), T(ok.astype(np.float32)),
-                        input_scales(float(np.max(activity)), float(dc.max())))
+                        input_scales(float(np.max(activity)), float(dc[tissue].max() if tissue.any() else dc.max())))
 
 
 def generate_training_pairs(n: int, shape=(64, 64, 64), voxel_mm: float = 4.0, radionuclide: str = "Y90",
@@ -432,8 +441,8 @@ def generate_training_pairs(n: int, shape=(64, 64, 64), voxel_mm: float = 4.0, r
 
 def train(net: UNet3D, pairs: Sequence[TrainingPair], steps: int, crop=(32, 32, 32), lr: float = 2e-3,
           seed: int = 0, log_every: int = 0) -> TrainStats:
-    """Adam on random crops (random flips are not used: the physics is not
-    mirror-symmetric once the crop origin is fixed, but the data are)."""
+    """Adam (cosine-decayed learning rate) on random crops of random pairs; a crop
+    lies inside its volume when it fits, else covers it from a random offset."""
     rng = np.random.default_rng(seed)
     ws = net.workspace(crop, train=True)
     stream = _stream_handle(None)
@@ -443,7 +452,7 @@ def train(net: UNet3D, pairs: Sequence[TrainingPair], steps: int, crop=(32, 32, 
     for it in range(steps):
         p = pairs[int(rng.integers(len(pairs)))]
         vd = p.activity.shape
-        origin = [int(rng.integers(-c // 4, max(1, vd[k] - 3 * c // 4))) for k, c in enumerate(crop)]
+        origin = [int(rng.integers(min(0, vd[k] - c), max(0, vd[k] - c) + 1)) for k, c in enumerate(crop)]
         net.pack_input(ws, (p.activity, p.density, p.dose_conv), p.scales, origin, stream)
         net.forward(ws, stream)
         net.backward(ws, p.target, p.weight, origin, stream)
@@ -469,7 +478,7 @@ def predict(net: UNet3D, activity: torch.Tensor, density: torch.Tensor, dose_con
     dev = net.device
     shape = tuple(activity.shape)
     if scales is None:
-        scales = input_scales(_vol_max(activity), _vol_max(dose_conv))
+        scales = _input_scales_device(activity, density, dose_conv)
     if out is None:
         out = torch.empty(shape, dtype=torch.float32, device=dev)
     fb = torch.empty(shape, dtype=torch.uint8, device=dev) if return_fallback else None
@@ -487,11 +496,14 @@ def predict(net: UNet3D, activity: torch.Tensor, density: torch.Tensor, dose_con
     return (out, fb) if return_fallback else out
 
 
-def dose_errors(dose: np.ndarray, reference: np.ndarray, rel_threshold: float = 0.1) -> Dict[str, float]:
-    """Relative errors |D - D_ref| / D_ref over voxels with D_ref > rel_threshold * max."""
+def dose_errors(dose: np.ndarray, reference: np.ndarray, rel_threshold: float = 0.1,
+                density: Optional[np.ndarray] = None) -> Dict[str, float]:
+    """Relative errors |D - D_ref| / D_ref over voxels with D_ref > rel_threshold
+    x max (max and voxels restricted to tissue when a density map is given)."""
     d = np.asarray(dose, np.float64)
     r = np.asarray(reference, np.float64)
-    m = r > rel_threshold * r.max()
+    sel = np.ones(r.shape, bool) if density is None else np.asarray(density) >= TISSUE_DENSITY
+    m = sel & (r > rel_threshold * r[sel].max())
     e = np.abs(d[m] - r[m]) / r[m]
     return {"mean": float(e.mean()), "median": float(np.median(e)), "p95": float(np.percentile(e, 95)),
             "max": float(e.max()), "within_3pct": float((e <= 0.03).mean()), "voxels": int(m.sum())}

@@ -592,7 +592,8 @@ __global__ void k_head(const uint8_t* __restrict__ x, long long plane, Geo g, co
 // loss and head backward.  pred: [2][n] from k_head; target/weight: full volumes
 // read at origin.  Per voxel e = mu - t, l = log(e^2 + eps):
 //   loss0 = sum w e^2 / n,  loss1 = sum w (s - l)^2 / n  (l taken as constant)
-// gx (16-channel planes) = (g_mu w0 + g_s w1) * leaky'(x); per-block partial sums
+// gx (16-channel planes) = g_mu w0 * leaky'(x): the error head s learns from the
+// features without passing its gradient into the network; per-block partial sums
 // of [dw0(16) dw1(16) db0 db1 loss0 loss1] go to part[block][36].
 constexpr int HEAD_THREADS = 256;
 __global__ void __launch_bounds__(HEAD_THREADS) k_head_loss(const uint8_t* __restrict__ x, long long plane, Geo g,
@@ -623,7 +624,7 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_head_loss(const uint8_t* __res
     unpack8(*reinterpret_cast<const uint4*>(x + plane + r), f + 8);
 #pragma unroll
     for (int c = 0; c < 16; ++c) {
-      gv[c] = (gm * w[c] + gs * w[16 + c]) * leaky_grad(f[c], slope);
+      gv[c] = gm * w[c] * leaky_grad(f[c], slope);
       acc[c] = gm * f[c];
       acc[16 + c] = gs * f[c];
     }
@@ -713,6 +714,28 @@ __global__ void k_apply(const float* __restrict__ pred, Geo g, const float* __re
   const bool fb = !(expf(0.5f * pred[n + i]) <= sigma_max);
   out[v] = fb ? dose[v] : dose[v] * expf(mu);
   if (fallback) fallback[v] = fb ? 1 : 0;
+}
+
+// maxima[0] = max activity, maxima[1] = max dose over voxels with density >= rho_min
+// (both over non-negative finite values; maxima zeroed first)
+__global__ void k_input_maxima(const float* __restrict__ act, const float* __restrict__ rho,
+                               const float* __restrict__ dose, long long n, float rho_min, float* maxima) {
+  float ma = 0.f, md = 0.f;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float a = act[i];
+    if (a > ma && a <= 3.4e38f) ma = a;
+    const float d = dose[i];
+    if (rho[i] >= rho_min && d > md && d <= 3.4e38f) md = d;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    ma = fmaxf(ma, __shfl_xor_sync(0xffffffffu, ma, o));
+    md = fmaxf(md, __shfl_xor_sync(0xffffffffu, md, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    // non-negative floats order like their bit patterns
+    atomicMax(reinterpret_cast<int*>(maxima), __float_as_int(ma));
+    atomicMax(reinterpret_cast<int*>(maxima) + 1, __float_as_int(md));
+  }
 }
 
 // Adam with decoupled weight decay on FP32 parameters
@@ -1073,6 +1096,17 @@ extern "C" pvd_status pvd_unet_apply_correction(const pvd_unet_geom* geom, const
                                                                vol_dims[0], vol_dims[1], vol_dims[2], sigma_max,
                                                                mu_clamp, dose_out, fallback);
   PVD_LAUNCH_CHECK("k_apply");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_input_maxima(const float* activity, const float* density, const float* dose, int64_t n,
+                                            float rho_min, float* maxima, pvd_stream stream) {
+  if (!activity || !density || !dose || !maxima || n < 0) return set_error(PVD_ERR_ARG, "pvd_unet_input_maxima: bad arguments");
+  PVD_CUDA_TRY(cudaMemsetAsync(maxima, 0, 2 * sizeof(float), (cudaStream_t)stream));
+  if (n == 0) return PVD_OK;
+  const unsigned grid = (unsigned)std::min<long long>(blocks_for(n, 256), 4LL * sm_count());
+  k_input_maxima<<<grid, 256, 0, (cudaStream_t)stream>>>(activity, density, dose, n, rho_min, maxima);
+  PVD_LAUNCH_CHECK("k_input_maxima");
   return PVD_OK;
 }
 
