@@ -50,6 +50,7 @@ LAYERS: List[Tuple[str, int, int]] = [
 ]
 LEVEL = {"e0a": 0, "e0b": 0, "e1a": 1, "e1b": 1, "e2a": 2, "e2b": 2, "e3a": 3, "e3b": 3,
          "d2a": 2, "d2b": 2, "d1a": 1, "d1b": 1, "d0a": 0, "d0b": 0}
+CHANNELS = {name: (ci, co) for name, ci, co in LAYERS}
 HEAD_SIZE = 34
 # input channels: activity / max (sqrt), density (linear), conv dose / max (sqrt)
 INPUT_MODES = (1, 0, 1)
@@ -230,20 +231,20 @@ class UNet3D:
 
     # --- layers -----------------------------------------------------------
     def _conv(self, name, x: _Tensor, y: _Tensor, stream) -> None:
-        _, ci, co = next(l for l in LAYERS if l[0] == name)
+        ci, co = CHANNELS[name]
         wo, bo, po = self.offsets[name]
         N.check(self._lib.pvd_unet_conv3d(C.byref(x.geom), x.ptr, ci, self._ptr(self.packed_fwd, po),
                                           self._ptr(self.params, bo), y.ptr, co, None, N.PVD_UNET_ACT_LEAKY,
                                           SLOPE, stream))
 
     def _dgrad(self, name, gy: _Tensor, dx: _Tensor, mask: Optional[_Tensor], stream) -> None:
-        _, ci, co = next(l for l in LAYERS if l[0] == name)
+        ci, co = CHANNELS[name]
         _, _, po = self.offsets[name]
         N.check(self._lib.pvd_unet_conv3d(C.byref(gy.geom), gy.ptr, co, self._ptr(self.packed_bwd, po), None,
                                           dx.ptr, ci, mask.ptr if mask is not None else None, 0, SLOPE, stream))
 
     def _wgrad(self, name, x: _Tensor, gy: _Tensor, ws: _Workspace, stream) -> None:
-        _, ci, co = next(l for l in LAYERS if l[0] == name)
+        ci, co = CHANNELS[name]
         wo, bo, _ = self.offsets[name]
         N.check(self._lib.pvd_unet_conv3d_wgrad(C.byref(x.geom), x.ptr, ci, gy.ptr, co, self._ptr(self.grads, wo), 0,
                                                 ws.scratch.data_ptr(), ws.scratch.numel(), stream))

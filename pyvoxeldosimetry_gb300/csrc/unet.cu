@@ -108,7 +108,7 @@ struct ConvArgs {
   const float* bias;    // [cout] or null
   uint8_t* y;           // output plane 0
   const uint8_t* mask;  // plane 0 of a cout-channel tensor whose LeakyReLU derivative scales the result, or null
-  int cin, cout, flags, nb, n_tiles;
+  int cin, cout, flags, na, nb, resident, n_tiles;
   float slope;
   long long plane;  // bytes per plane (rows * 16), same for x, y, mask
   Geo g;
@@ -119,12 +119,13 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
   const int cin8 = a.cin >> 3;
   const uint32_t a_bytes = (uint32_t)cin8 * SLAB_PITCH;
   const uint32_t b_bytes = (uint32_t)a.cin * a.cout * 2;
-  const int nb = a.nb;
+  const int na = a.na, nb = a.nb;
+  const bool resident = a.resident != 0;  // all 27 taps' weights loaded once into nb == 27 slots
   uint8_t* sa = sm;
-  uint8_t* sb = sm + 2 * a_bytes;
+  uint8_t* sb = sm + (size_t)na * a_bytes;
   uint64_t* full_a = reinterpret_cast<uint64_t*>(sb + (size_t)nb * b_bytes);
-  uint64_t* empty_a = full_a + 2;
-  uint64_t* full_b = empty_a + 2;
+  uint64_t* empty_a = full_a + na;
+  uint64_t* full_b = empty_a + na;
   uint64_t* empty_b = full_b + nb;
   uint64_t* acc_full = empty_b + nb;
   uint64_t* acc_empty = acc_full + 2;
@@ -133,9 +134,11 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
   const uint32_t ncols = umma::tmem_cols(2 * a.cout);
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < na; ++i) {
       mbar_init(&full_a[i], 1);
       mbar_init(&empty_a[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
       mbar_init(&acc_full[i], 1);
       mbar_init(&acc_empty[i], 128);
     }
@@ -154,14 +157,19 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
 
   if (warp == 0) {
     if (lane == 0) {
+      if (resident) {  // every tap's weights once, completing on full_b[0]
+        mbar_arrive_expect_tx(&full_b[0], 27 * b_bytes);
+        for (int tap = 0; tap < 27; ++tap)
+          umma::bulk_g2s(sb + (size_t)tap * b_bytes, a.w + (size_t)tap * b_bytes, b_bytes, &full_b[0]);
+      }
       int it_a = 0, it_b = 0;
       for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
         const long long p0 = (long long)tile * TILE_M;
         for (int grp = 0; grp < 9; ++grp) {
           const int dz = grp / 3, dy = grp % 3;
           const long long row0 = g.margin + p0 + (long long)(dz - 1) * g.Hp * g.Wp + (long long)(dy - 1) * g.Wp - 1;
-          const int s = it_a & 1;
-          if (!mbar_wait_bounded(&empty_a[s], ((it_a >> 1) & 1) ^ 1, WAIT_NS)) {
+          const int s = it_a % na;
+          if (!mbar_wait_bounded(&empty_a[s], ((it_a / na) & 1) ^ 1, WAIT_NS)) {
             fail(ST_TIMEOUT_LOAD);
             goto done;
           }
@@ -170,6 +178,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
             umma::bulk_g2s(sa + (size_t)s * a_bytes + (size_t)c * SLAB_PITCH, a.x + c * a.plane + row0 * 16, SLAB_PITCH,
                            &full_a[s]);
           ++it_a;
+          if (resident) continue;
           for (int dx = 0; dx < 3; ++dx) {
             const int tap = grp * 3 + dx;
             const int sbi = it_b % nb;
@@ -189,6 +198,10 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
       const uint32_t idesc = umma::idesc_bf16(a.cout, false, false);
       const uint32_t b_lbo = (uint32_t)a.cout * 16;
       int it_a = 0, it_b = 0, t_local = 0;
+      if (resident && !mbar_wait_bounded(&full_b[0], 0, WAIT_NS)) {
+        fail(ST_TIMEOUT_MMA);
+        goto done;
+      }
       for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++t_local) {
         const int acc = t_local & 1;
         if (!mbar_wait_bounded(&acc_empty[acc], ((t_local >> 1) & 1) ^ 1, WAIT_NS)) {
@@ -198,28 +211,32 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
         umma::fence_after_sync();
         const uint32_t d = tmem + (uint32_t)(acc * a.cout);
         for (int grp = 0; grp < 9; ++grp) {
-          const int s = it_a & 1;
-          if (!mbar_wait_bounded(&full_a[s], (it_a >> 1) & 1, WAIT_NS)) {
+          const int s = it_a % na;
+          if (!mbar_wait_bounded(&full_a[s], (it_a / na) & 1, WAIT_NS)) {
             fail(ST_TIMEOUT_MMA);
             goto done;
           }
           umma::fence_after_sync();
           const uint32_t abase = smem_u32(sa + (size_t)s * a_bytes);
           for (int dx = 0; dx < 3; ++dx) {
-            const int sbi = it_b % nb;
-            if (!mbar_wait_bounded(&full_b[sbi], (it_b / nb) & 1, WAIT_NS)) {
-              fail(ST_TIMEOUT_MMA);
-              goto done;
+            const int sbi = resident ? grp * 3 + dx : it_b % nb;
+            if (!resident) {
+              if (!mbar_wait_bounded(&full_b[sbi], (it_b / nb) & 1, WAIT_NS)) {
+                fail(ST_TIMEOUT_MMA);
+                goto done;
+              }
+              umma::fence_after_sync();
             }
-            umma::fence_after_sync();
             const uint32_t bbase = smem_u32(sb + (size_t)sbi * b_bytes);
             for (int kc = 0; kc < a.cin / 16; ++kc) {
               const uint64_t ad = umma::smem_desc(abase + dx * 16 + 2 * kc * SLAB_PITCH, SLAB_PITCH, 128);
               const uint64_t bd = umma::smem_desc(bbase + 2 * kc * b_lbo, b_lbo, 128);
               umma::mma_bf16(d, ad, bd, idesc, (grp | dx | kc) != 0);
             }
-            umma::commit(&empty_b[sbi]);
-            ++it_b;
+            if (!resident) {
+              umma::commit(&empty_b[sbi]);
+              ++it_b;
+            }
           }
           umma::commit(&empty_a[s]);
           ++it_a;
@@ -244,6 +261,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
       const long long roff = (g.margin + p) * 16;
       for (int c0 = 0; c0 < a.cout; c0 += 16) {
         float v[16];
+        __syncwarp();
         umma::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * a.cout + c0), v);
         if (a.bias) {
 #pragma unroll
@@ -412,16 +430,20 @@ done:
 }
 
 // dw[n][k][tap] = sum over splits of partial[split][mt][m][n], m_global = tap*cin + k = mt*128 + m
+// (threads run along n, so every split's partial row is read contiguously)
 __global__ void k_wgrad_reduce(const float* __restrict__ partial, float* __restrict__ dw, int cin, int cout,
                                int m_tiles, int splits, int accumulate) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int total = cout * cin * 27;
   if (i >= total) return;
-  const int tap = i % 27, k = (i / 27) % cin, n = i / (27 * cin);
-  const int mgl = tap * cin + k, mt = mgl / 128, m = mgl % 128;
+  const int n = i % cout, mgl = i / cout;
+  const int tap = mgl / cin, k = mgl % cin;
+  const size_t stride = (size_t)m_tiles * 128 * cout;
+  const float* src = partial + (size_t)mgl * cout + n;  // mt * 128 + m == mgl
   float s = 0.f;
-  for (int sp = 0; sp < splits; ++sp) s += partial[(((size_t)sp * m_tiles + mt) * 128 + m) * cout + n];
-  dw[i] = accumulate ? dw[i] + s : s;
+  for (int sp = 0; sp < splits; ++sp) s += src[sp * stride];
+  const size_t o = ((size_t)n * cin + k) * 27 + tap;
+  dw[o] = accumulate ? dw[o] + s : s;
 }
 
 // ---------------------------------------------------------------------------
@@ -769,8 +791,33 @@ static int sm_count() {
 static bool ch_ok(int c) { return c >= 16 && c <= 256 && c % 16 == 0; }
 static bool al16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
-static size_t conv_smem(int cin, int cout, int nb) {
-  return 2 * (size_t)(cin / 8) * SLAB_PITCH + (size_t)nb * cin * cout * 2 + (size_t)(8 + 2 * nb) * 8 + 16;
+static size_t conv_smem(int cin, int cout, int na, int nb) {
+  return (size_t)na * (cin / 8) * SLAB_PITCH + (size_t)nb * cin * cout * 2 + (size_t)(4 + 2 * na + 2 * nb) * 8 + 16;
+}
+
+// Shared-memory plan of a convolution: all 27 taps' weights resident with up to
+// four input slabs in flight when they fit, else a ring of tap-weight slots.
+struct ConvPlanSm {
+  int na, nb, resident, occ;
+  size_t smem;
+};
+
+static ConvPlanSm conv_plan(int cin, int cout) {
+  ConvPlanSm p{0, 0, 0, 0, 0};
+  // resident weights: the deepest input-slab ring (up to a whole tile's 9 slabs) that
+  // still lets 4, else 2, else 1 CTAs share an SM
+  for (int target : {4, 2, 1}) {
+    const size_t budget = std::min((size_t)MAX_SMEM, (size_t)(233472 / target) - 2048);
+    for (int na = 9; na >= 2 && !p.na; --na)
+      if (conv_smem(cin, cout, na, 27) <= budget) p = {na, 27, 1, 0, conv_smem(cin, cout, na, 27)};
+    if (p.na) break;
+  }
+  if (!p.na) {
+    int nb = 4;
+    while (nb > 2 && conv_smem(cin, cout, 2, nb) > (size_t)MAX_SMEM) --nb;
+    p = {2, nb, 0, 0, conv_smem(cin, cout, 2, nb)};
+  }
+  return p;
 }
 
 static pvd_status geo_check(const pvd_unet_geom* g) {
@@ -814,10 +861,34 @@ extern "C" pvd_status pvd_unet_conv3d(const pvd_unet_geom* geom, const void* x, 
   if (!x || !w_packed || !y || !al16(x) || !al16(w_packed) || !al16(y) || (mask && !al16(mask)))
     return set_error(PVD_ERR_ARG, "pvd_unet_conv3d: tensors must be non-null and 16-byte aligned");
   if (flags & ~(PVD_UNET_ACT_LEAKY | PVD_UNET_ACCUMULATE)) return set_error(PVD_ERR_ARG, "pvd_unet_conv3d: unknown flags");
-  int nb = 4;
-  while (nb > 2 && conv_smem(cin, cout, nb) > (size_t)MAX_SMEM) --nb;
-  const size_t smem = conv_smem(cin, cout, nb);
-  if (smem > (size_t)MAX_SMEM) return set_error(PVD_ERR_UNSUPPORTED, "pvd_unet_conv3d: channel counts need more shared memory than a CTA has");
+  // launch configuration per (cin, cout), computed once per process (one device)
+  static ConvPlanSm plans[17][17];
+  static bool have[17][17];
+  ConvPlanSm& pl = plans[cin / 16][cout / 16];
+  if (!have[cin / 16][cout / 16]) {
+    pl = conv_plan(cin, cout);
+    if (pl.smem > (size_t)MAX_SMEM)
+      return set_error(PVD_ERR_UNSUPPORTED, "pvd_unet_conv3d: channel counts need more shared memory than a CTA has");
+    PVD_CUDA_TRY(cudaFuncSetAttribute(k_conv3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MAX_SMEM));
+    // CTAs that can be resident on one SM at once: registers (allocated per warp in
+    // units of 256), shared memory (228 KB per SM, 1 KB reserved per CTA), threads,
+    // and TMEM (512 columns per SM; a CTA holds two accumulators of cout columns)
+    cudaFuncAttributes fa;
+    PVD_CUDA_TRY(cudaFuncGetAttributes(&fa, k_conv3));
+    const int regs_warp = (fa.numRegs * 32 + 255) / 256 * 256;
+    const int by_regs = 65536 / (regs_warp * (CONV_THREADS / 32));
+    const int by_smem = (int)(233472 / (pl.smem + fa.sharedSizeBytes + 1024));
+    const int by_threads = 2048 / CONV_THREADS;
+    const int by_tmem = (int)(512 / umma::tmem_cols(2 * cout));
+    pl.occ = std::max(1, std::min(std::min(by_regs, by_smem), std::min(by_threads, by_tmem)));
+    // when TMEM is the binding limit, request enough shared memory that no more CTAs
+    // than that can be co-resident (an extra CTA would wait in tcgen05.alloc for a
+    // persistent CTA to finish)
+    if (by_tmem < std::min(std::min(by_regs, by_smem), by_threads))
+      pl.smem = std::max(pl.smem, (size_t)(233472 / by_tmem) - 1024 - fa.sharedSizeBytes);
+    have[cin / 16][cout / 16] = true;
+  }
+  const size_t smem = pl.smem;
   ConvArgs a;
   a.x = (const uint8_t*)x;
   a.w = (const uint8_t*)w_packed;
@@ -827,17 +898,14 @@ extern "C" pvd_status pvd_unet_conv3d(const pvd_unet_geom* geom, const void* x, 
   a.cin = cin;
   a.cout = cout;
   a.flags = flags;
-  a.nb = nb;
+  a.na = pl.na;
+  a.nb = pl.nb;
+  a.resident = pl.resident;
   a.slope = slope;
   a.g = make_geo(geom);
   a.plane = a.g.rows * 16;
   a.n_tiles = (int)(a.g.np_tiles / TILE_M);
-  PVD_CUDA_TRY(cudaFuncSetAttribute(k_conv3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int occ = 1;
-  PVD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv3, CONV_THREADS, smem));
-  const int by_tmem = (int)(512 / umma::tmem_cols(2 * cout));
-  occ = std::max(1, std::min(occ, by_tmem));
-  const int grid = std::min(a.n_tiles, sm_count() * occ);
+  const int grid = std::min(a.n_tiles, sm_count() * pl.occ);
   k_conv3<<<grid, CONV_THREADS, smem, (cudaStream_t)stream>>>(a);
   PVD_LAUNCH_CHECK("k_conv3");
   return PVD_OK;

@@ -95,6 +95,39 @@ def test_conv_forward(env, cin, cout):
     assert _halo_zero(y, lc)
 
 
+@pytest.mark.parametrize("cin,cout,mode", [(16, 16, "fwd"), (128, 128, "fwd"), (192, 64, "fwd"),
+                                            (96, 32, "dgrad"), (64, 192, "dgrad")])
+def test_conv_persistent_many_tiles(env, cin, cout, mode):
+    """1170 row tiles: more than one tile per persistent CTA, both weight modes
+    (all taps resident for the small layers, a ring of tap slots for the large)."""
+    N, lc, lib, dev = env
+    dims = (46, 50, 58)
+    gen = torch.Generator().manual_seed(3 * cin + cout)
+    g = lc.geometry(dims)
+    X = _dense(cin, dims, gen)
+    W = torch.randn(cout, cin, 27, generator=gen, dtype=torch.float64) * np.sqrt(2.0 / (27 * cin))
+    x = lc._Tensor.zeros(cin, g, dev)
+    x.load_dense(X.float().to(dev))
+    y = lc._Tensor.zeros(cout, g, dev)
+    packed = torch.zeros(27 * cin * cout, dtype=torch.bfloat16, device=dev)
+    if mode == "fwd":
+        N.check(lib.pvd_unet_pack_weights(W.float().to(dev).data_ptr(), cin, cout, packed.data_ptr(), None, None))
+        N.check(lib.pvd_unet_conv3d(C.byref(g), x.ptr, cin, packed.data_ptr(), None, y.ptr, cout, None,
+                                    N.PVD_UNET_ACT_LEAKY, 0.01, None))
+        ref = F.leaky_relu(F.conv3d(X[None], _bf(W).reshape(cout, cin, 3, 3, 3), padding=1), 0.01)[0]
+    else:  # the data gradient of a cout -> cin convolution: run cin -> cout on the mirrored packing
+        Wt = torch.randn(cin, cout, 27, generator=gen, dtype=torch.float64) * 0.05
+        N.check(lib.pvd_unet_pack_weights(Wt.float().to(dev).data_ptr(), cout, cin, None, packed.data_ptr(), None))
+        N.check(lib.pvd_unet_conv3d(C.byref(g), x.ptr, cin, packed.data_ptr(), None, y.ptr, cout, None, 0, 0.01,
+                                    None))
+        ref = torch.nn.grad.conv3d_input((1, cout) + dims, _bf(Wt).reshape(cin, cout, 3, 3, 3), X[None],
+                                         padding=1)[0]
+    code = C.c_int()
+    N.check(lib.pvd_unet_status(C.byref(code), 1))
+    _check_bf16(y.to_dense(), ref, f"{mode} {cin}->{cout} many tiles")
+    assert _halo_zero(y, lc)
+
+
 @pytest.mark.parametrize("cin,cout", [(16, 16), (48, 16), (96, 32), (192, 64), (128, 128)])
 def test_conv_data_gradient(env, cin, cout):
     """Input gradient of a cin -> cout conv: the kernel run cout -> cin on the
