@@ -430,30 +430,9 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
     dcn = dc.cpu().numpy()
     pair = lc.make_pair(act, rho, dcn, dcn * 1.1, device=device)
     net = lc.UNet3D(seed=1, device=device)
-    lc.train(net, [pair], 3, crop=crop)
-    s = torch.cuda.current_stream().cuda_stream
-    ws = net.workspace(crop, train=True)
-
-    def one_step():
-        net.pack_input(ws, (pair.activity, pair.density, pair.dose_conv), pair.scales, (0, 0, 0), s)
-        net.forward(ws, s)
-        net.backward(ws, pair.target, pair.weight, (0, 0, 0), s)
-        net.adam(lr=1e-4)
-
-    one_step()
+    # inference first (so a launch list of this run starts with it): plain conv +
+    # network + apply on the whole phantom
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record()
-    for _ in range(train_steps):
-        one_step()
-    e1.record()
-    e1.synchronize()
-    step_ms = e0.elapsed_time(e1) / train_steps
-    # forward + data gradient (all but the first layer) + weight gradient
-    fwd = lc.conv_flops(crop)
-    first = 2.0 * 27 * 16 * 16 * crop[0] * crop[1] * crop[2]
-    step_flops = 3 * fwd - first
-    # inference: plain conv + network + apply on the whole phantom
     out = torch.empty_like(dc)
     lc.predict(net, a, r, dc, out=out)
     inf_ms, conv_ms = [], []
@@ -469,6 +448,28 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
         e1.synchronize()
         inf_ms.append(e0.elapsed_time(e1))
     conv_t, inf_t = float(np.median(conv_ms)), float(np.median(inf_ms))
+    lc.train(net, [pair], 3, crop=crop)
+    s = torch.cuda.current_stream().cuda_stream
+    ws = net.workspace(crop, train=True)
+
+    def one_step():
+        net.pack_input(ws, (pair.activity, pair.density, pair.dose_conv), pair.scales, (0, 0, 0), s)
+        net.forward(ws, s)
+        net.backward(ws, pair.target, pair.weight, (0, 0, 0), s)
+        net.adam(lr=1e-4)
+
+    one_step()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(train_steps):
+        one_step()
+    e1.record()
+    e1.synchronize()
+    step_ms = e0.elapsed_time(e1) / train_steps
+    # forward + data gradient (all but the first layer) + weight gradient
+    fwd = lc.conv_flops(crop)
+    first = 2.0 * 27 * 16 * 16 * crop[0] * crop[1] * crop[2]
+    step_flops = 3 * fwd - first
     infer_crop = tuple(-(-n // 8) * 8 for n in shape)
     nvox = float(np.prod(shape))
     # Monte Carlo to 1 %: 10 batches, relative standard error of the mean per voxel
@@ -484,6 +485,7 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
     mc_ms = e0.elapsed_time(e1)
     plan.close()
     conv.close()
+    net.status()
     st = np.stack(batches)
     mean = st.mean(0)
     sel = mean > 0.1 * mean.max()

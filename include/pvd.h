@@ -532,12 +532,13 @@ pvd_status pvd_unet_pack_weights(const float* w, int cin, int cout, void* fwd_pa
                                  pvd_stream stream);
 
 /* Network input (16 channels): channel c < n_in (<= 4) is volumes[c] (device
- * float32, C order, vol_dims) read at origin + voxel, times scales[c], then
+ * float32, C order, vol_dims) read at origin + voxel, times scales[c] (host) or,
+ * when scales_d is not NULL, scales_d[c] (device, read by the kernel), then
  * modes[c]: 0 linear, 1 sqrt, 2 log1p; channels >= n_in are zero, and so is
  * every channel of a voxel outside the volumes (a crop may overhang them). */
 pvd_status pvd_unet_pack_input(const pvd_unet_geom* geom, const float* const* volumes, const float* scales,
-                               const int* modes, int n_in, const int* vol_dims, const int* origin, void* x,
-                               pvd_stream stream);
+                               const float* scales_d, const int* modes, int n_in, const int* vol_dims,
+                               const int* origin, void* x, pvd_stream stream);
 
 /* 2x2x2 average pooling (fine dims = 2 x coarse dims) and its backward:
  * dx = ((accumulate ? dx : 0) + dy[parent] / 8) * (mask ? leaky'(mask) : 1). */
@@ -580,9 +581,10 @@ pvd_status pvd_unet_apply_correction(const pvd_unet_geom* geom, const float* pre
                                      const int* vol_dims, const int* origin, float sigma_max, float mu_clamp,
                                      float* dose_out, uint8_t* fallback, pvd_stream stream);
 
-/* maxima_d[0] = max activity, maxima_d[1] = max dose over voxels with
- * density >= rho_min (device float32 volumes of n voxels; non-negative finite
- * values; 0 if none).  The network input is scaled by their reciprocals. */
+/* maxima_d (device, 5 floats): [0] = max activity, [1] = max dose over voxels
+ * with density >= rho_min (device float32 volumes of n voxels; non-negative
+ * finite values; 0 if none), [2..4] = the network input scales 1/[0], 1, 1/[1]
+ * (0 where the maximum is 0), ready for pvd_unet_pack_input's scales_d. */
 pvd_status pvd_unet_input_maxima(const float* activity, const float* density, const float* dose, int64_t n,
                                  float rho_min, float* maxima_d, pvd_stream stream);
 

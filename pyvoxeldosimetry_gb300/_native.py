@@ -176,7 +176,7 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_unet_wgrad_workspace": (st, [C.POINTER(UnetGeom), i, i, C.POINTER(C.c_size_t)]),
         "pvd_unet_conv3d_wgrad": (st, [C.POINTER(UnetGeom), vp, i, vp, i, vp, i, vp, C.c_size_t, vp]),
         "pvd_unet_pack_weights": (st, [vp, i, i, vp, vp, vp]),
-        "pvd_unet_pack_input": (st, [C.POINTER(UnetGeom), C.POINTER(vp), C.POINTER(f), C.POINTER(i), i,
+        "pvd_unet_pack_input": (st, [C.POINTER(UnetGeom), C.POINTER(vp), C.POINTER(f), vp, C.POINTER(i), i,
                                      C.POINTER(i), C.POINTER(i), vp, vp]),
         "pvd_unet_pool": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), vp, i, vp]),
         "pvd_unet_pool_backward": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), vp, vp, i, i, f, vp]),

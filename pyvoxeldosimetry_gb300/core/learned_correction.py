@@ -258,16 +258,20 @@ class UNet3D:
         N.check(self._lib.pvd_unet_upsample(C.byref(x.geom), x.ptr, C.byref(y.geom), y.ptr, x.channels, stream))
 
     # --- passes -----------------------------------------------------------
-    def pack_input(self, ws: _Workspace, volumes: Sequence[torch.Tensor], scales: Sequence[float], origin,
-                   stream) -> None:
+    def pack_input(self, ws: _Workspace, volumes: Sequence[torch.Tensor], scales, origin, stream) -> None:
+        """scales: host floats, or a device float32 tensor of len(volumes) scales."""
         vd = volumes[0].shape
         n = len(volumes)
         vp = (C.c_void_p * n)(*[v.data_ptr() for v in volumes])
-        sc = (C.c_float * n)(*[float(s) for s in scales])
+        if isinstance(scales, torch.Tensor):
+            sc, sc_d = None, scales.data_ptr()
+        else:
+            sc, sc_d = (C.c_float * n)(*[float(s) for s in scales]), None
         md = (C.c_int * n)(*INPUT_MODES[:n])
         dims = (C.c_int * 3)(*[int(d) for d in vd])
         org = (C.c_int * 3)(*[int(o) for o in origin])
-        N.check(self._lib.pvd_unet_pack_input(C.byref(ws.geo[0]), vp, sc, md, n, dims, org, ws.t["x0"].ptr, stream))
+        N.check(self._lib.pvd_unet_pack_input(C.byref(ws.geo[0]), vp, sc, sc_d, md, n, dims, org, ws.t["x0"].ptr,
+                                              stream))
 
     def forward(self, ws: _Workspace, stream) -> torch.Tensor:
         """Run the network on ws.t['x0']; returns pred [2 * D*H*W] (mu then s)."""
@@ -383,13 +387,13 @@ def input_scales(activity_max: float, dose_max: float) -> Tuple[float, float, fl
 TISSUE_DENSITY = 0.2  # g/cc: lung and denser; dose to air is not a target
 
 
-def _input_scales_device(activity: torch.Tensor, density: torch.Tensor, dose: torch.Tensor):
-    """input_scales from the device maxima of activity and of the dose over tissue."""
-    mx = torch.empty(2, dtype=torch.float32, device=activity.device)
+def _input_scales_device(activity: torch.Tensor, density: torch.Tensor, dose: torch.Tensor) -> torch.Tensor:
+    """The input scales of ``input_scales`` computed on the device (no host round
+    trip): a float32 tensor [1/max activity, 1, 1/max dose over tissue]."""
+    mx = torch.empty(5, dtype=torch.float32, device=activity.device)
     N.check(N.load().pvd_unet_input_maxima(activity.data_ptr(), density.data_ptr(), dose.data_ptr(), activity.numel(),
                                            TISSUE_DENSITY, mx.data_ptr(), _stream_handle(None)))
-    m = mx.cpu()
-    return input_scales(float(m[0]), float(m[1]))
+    return mx[2:5]
 
 
 def make_pair(activity: np.ndarray, density: np.ndarray, dose_conv: np.ndarray, dose_mc: np.ndarray,
@@ -475,7 +479,9 @@ def predict(net: UNet3D, activity: torch.Tensor, density: torch.Tensor, dose_con
             return_fallback: bool = False):
     """Corrected dose for a whole volume (device float32 tensors of one shape).
     The network runs on one crop covering the volume, its dims rounded up to
-    multiples of 8 (the overhang reads as zero input)."""
+    multiples of 8 (the overhang reads as zero input).  Everything is enqueued on
+    the current stream without a host round trip; ``net.status()`` reads the
+    tensor-core pipeline's status word afterwards."""
     dev = net.device
     shape = tuple(activity.shape)
     if scales is None:
@@ -493,7 +499,6 @@ def predict(net: UNet3D, activity: torch.Tensor, density: torch.Tensor, dose_con
     N.check(net._lib.pvd_unet_apply_correction(C.byref(ws.geo[0]), pred.data_ptr(), dose_conv.data_ptr(), vd, org,
                                                sigma_max, mu_clamp, out.data_ptr(),
                                                fb.data_ptr() if fb is not None else None, stream))
-    net.status()
     return (out, fb) if return_fallback else out
 
 
@@ -564,6 +569,7 @@ class NNCorrectedDoseCalculator(DosimetryCalculator):
         rho = _io.to_device(density, dev, "density")
         dc = self.conv.calculate_dose_rate(a, voxel_size, density=rho)
         out, self._fb = predict(self.model, a, rho, dc, sigma_max=self.sigma_max, return_fallback=True)
+        self.model.status()
         return _io.from_device(out, kind)
 
     def fallback_fraction(self) -> float:

@@ -156,93 +156,96 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
   const Geo& g = a.g;
 
   if (warp == 0) {
-    if (lane == 0) {
-      if (resident) {  // every tap's weights once, completing on full_b[0]
-        mbar_arrive_expect_tx(&full_b[0], 27 * b_bytes);
-        for (int tap = 0; tap < 27; ++tap)
-          umma::bulk_g2s(sb + (size_t)tap * b_bytes, a.w + (size_t)tap * b_bytes, b_bytes, &full_b[0]);
-      }
-      int it_a = 0, it_b = 0;
-      for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
-        const long long p0 = (long long)tile * TILE_M;
-        for (int grp = 0; grp < 9; ++grp) {
-          const int dz = grp / 3, dy = grp % 3;
-          const long long row0 = g.margin + p0 + (long long)(dz - 1) * g.Hp * g.Wp + (long long)(dy - 1) * g.Wp - 1;
-          const int s = it_a % na;
-          if (!mbar_wait_bounded(&empty_a[s], ((it_a / na) & 1) ^ 1, WAIT_NS)) {
-            fail(ST_TIMEOUT_LOAD);
+    // load warp: lane 0 waits and arms the barrier, lane c copies plane c of the slab
+    if (resident) {  // every tap's weights once, completing on full_b[0]
+      if (lane == 0) mbar_arrive_expect_tx(&full_b[0], 27 * b_bytes);
+      __syncwarp();
+      if (lane < 27) umma::bulk_g2s(sb + (size_t)lane * b_bytes, a.w + (size_t)lane * b_bytes, b_bytes, &full_b[0]);
+    }
+    int it_a = 0, it_b = 0;
+    for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+      const long long p0 = (long long)tile * TILE_M;
+      for (int grp = 0; grp < 9; ++grp) {
+        const int dz = grp / 3, dy = grp % 3;
+        const long long row0 = g.margin + p0 + (long long)(dz - 1) * g.Hp * g.Wp + (long long)(dy - 1) * g.Wp - 1;
+        const int s = it_a % na;
+        if (!umma::warp_wait(&empty_a[s], ((it_a / na) & 1) ^ 1, WAIT_NS)) {
+          if (lane == 0) fail(ST_TIMEOUT_LOAD);
+          goto done;
+        }
+        if (lane == 0) mbar_arrive_expect_tx(&full_a[s], a_bytes);
+        __syncwarp();
+        for (int c = lane; c < cin8; c += 32)
+          umma::bulk_g2s(sa + (size_t)s * a_bytes + (size_t)c * SLAB_PITCH, a.x + c * a.plane + row0 * 16, SLAB_PITCH,
+                         &full_a[s]);
+        ++it_a;
+        if (resident) continue;
+        for (int dx = 0; dx < 3; ++dx) {
+          const int tap = grp * 3 + dx;
+          const int sbi = it_b % nb;
+          if (!umma::warp_wait(&empty_b[sbi], ((it_b / nb) & 1) ^ 1, WAIT_NS)) {
+            if (lane == 0) fail(ST_TIMEOUT_LOAD);
             goto done;
           }
-          mbar_arrive_expect_tx(&full_a[s], a_bytes);
-          for (int c = 0; c < cin8; ++c)
-            umma::bulk_g2s(sa + (size_t)s * a_bytes + (size_t)c * SLAB_PITCH, a.x + c * a.plane + row0 * 16, SLAB_PITCH,
-                           &full_a[s]);
-          ++it_a;
-          if (resident) continue;
-          for (int dx = 0; dx < 3; ++dx) {
-            const int tap = grp * 3 + dx;
-            const int sbi = it_b % nb;
-            if (!mbar_wait_bounded(&empty_b[sbi], ((it_b / nb) & 1) ^ 1, WAIT_NS)) {
-              fail(ST_TIMEOUT_LOAD);
-              goto done;
-            }
+          if (lane == 0) {
             mbar_arrive_expect_tx(&full_b[sbi], b_bytes);
             umma::bulk_g2s(sb + (size_t)sbi * b_bytes, a.w + (size_t)tap * b_bytes, b_bytes, &full_b[sbi]);
-            ++it_b;
           }
+          __syncwarp();
+          ++it_b;
         }
       }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
-      const uint32_t idesc = umma::idesc_bf16(a.cout, false, false);
-      const uint32_t b_lbo = (uint32_t)a.cout * 16;
-      int it_a = 0, it_b = 0, t_local = 0;
-      if (resident && !mbar_wait_bounded(&full_b[0], 0, WAIT_NS)) {
-        fail(ST_TIMEOUT_MMA);
+    // MMA warp: the whole warp walks the loop (uniform descriptors), one elected lane issues
+    const uint32_t idesc = umma::idesc_bf16(a.cout, false, false);
+    const uint32_t b_lbo = (uint32_t)a.cout * 16;
+    const uint64_t a_kstep = (2 * SLAB_PITCH) >> 4;  // descriptor start-address units per 16 channels
+    const uint64_t b_kstep = (2 * b_lbo) >> 4;
+    const int ksteps = a.cin / 16;
+    int it_a = 0, it_b = 0, t_local = 0;
+    if (resident && !umma::warp_wait(&full_b[0], 0, WAIT_NS)) {
+      if (lane == 0) fail(ST_TIMEOUT_MMA);
+      goto done;
+    }
+    for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++t_local) {
+      const int acc = t_local & 1;
+      if (!umma::warp_wait(&acc_empty[acc], ((t_local >> 1) & 1) ^ 1, WAIT_NS)) {
+        if (lane == 0) fail(ST_TIMEOUT_MMA);
         goto done;
       }
-      for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++t_local) {
-        const int acc = t_local & 1;
-        if (!mbar_wait_bounded(&acc_empty[acc], ((t_local >> 1) & 1) ^ 1, WAIT_NS)) {
-          fail(ST_TIMEOUT_MMA);
+      umma::fence_after_sync();
+      const uint32_t d = tmem + (uint32_t)(acc * a.cout);
+      for (int grp = 0; grp < 9; ++grp) {
+        const int s = it_a % na;
+        if (!umma::warp_wait(&full_a[s], (it_a / na) & 1, WAIT_NS)) {
+          if (lane == 0) fail(ST_TIMEOUT_MMA);
           goto done;
         }
         umma::fence_after_sync();
-        const uint32_t d = tmem + (uint32_t)(acc * a.cout);
-        for (int grp = 0; grp < 9; ++grp) {
-          const int s = it_a % na;
-          if (!mbar_wait_bounded(&full_a[s], (it_a / na) & 1, WAIT_NS)) {
-            fail(ST_TIMEOUT_MMA);
-            goto done;
+        const uint64_t a0 = umma::smem_desc(smem_u32(sa + (size_t)s * a_bytes), SLAB_PITCH, 128);
+        for (int dx = 0; dx < 3; ++dx) {
+          const int sbi = resident ? grp * 3 + dx : it_b % nb;
+          if (!resident) {
+            if (!umma::warp_wait(&full_b[sbi], (it_b / nb) & 1, WAIT_NS)) {
+              if (lane == 0) fail(ST_TIMEOUT_MMA);
+              goto done;
+            }
+            umma::fence_after_sync();
           }
-          umma::fence_after_sync();
-          const uint32_t abase = smem_u32(sa + (size_t)s * a_bytes);
-          for (int dx = 0; dx < 3; ++dx) {
-            const int sbi = resident ? grp * 3 + dx : it_b % nb;
-            if (!resident) {
-              if (!mbar_wait_bounded(&full_b[sbi], (it_b / nb) & 1, WAIT_NS)) {
-                fail(ST_TIMEOUT_MMA);
-                goto done;
-              }
-              umma::fence_after_sync();
-            }
-            const uint32_t bbase = smem_u32(sb + (size_t)sbi * b_bytes);
-            for (int kc = 0; kc < a.cin / 16; ++kc) {
-              const uint64_t ad = umma::smem_desc(abase + dx * 16 + 2 * kc * SLAB_PITCH, SLAB_PITCH, 128);
-              const uint64_t bd = umma::smem_desc(bbase + 2 * kc * b_lbo, b_lbo, 128);
-              umma::mma_bf16(d, ad, bd, idesc, (grp | dx | kc) != 0);
-            }
-            if (!resident) {
-              umma::commit(&empty_b[sbi]);
-              ++it_b;
-            }
+          uint64_t ad = a0 + (uint64_t)dx;  // +16 bytes per dx tap
+          uint64_t bd = umma::smem_desc(smem_u32(sb + (size_t)sbi * b_bytes), b_lbo, 128);
+          for (int kc = 0; kc < ksteps; ++kc, ad += a_kstep, bd += b_kstep)
+            umma::mma_bf16_elect(d, ad, bd, idesc, (grp | dx | kc) != 0);
+          if (!resident) {
+            umma::commit_elect(&empty_b[sbi]);
+            ++it_b;
           }
-          umma::commit(&empty_a[s]);
-          ++it_a;
         }
-        umma::commit(&acc_full[acc]);
+        umma::commit_elect(&empty_a[s]);
+        ++it_a;
       }
+      umma::commit_elect(&acc_full[acc]);
     }
   } else {
     // epilogue: warp w reads TMEM lanes 32*(w%4) .. +31, one output row per thread
@@ -352,54 +355,55 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_wgrad(const WgradArgs a) {
   const uint32_t tmem = *tslot;
 
   if (warp == 0) {
-    if (lane == 0) {
-      // source rows of the 16 A groups (tap, 8-channel chunk) of this M tile
-      long long a_off[16];
-      int a_pl[16];
-      for (int grp = 0; grp < 16; ++grp) {
-        const int mg = mt * 128 + grp * 8;
-        int tap = mg / a.cin, ch = (mg % a.cin) / 8;
-        if (tap >= 27) tap = 0, ch = 0;  // rows beyond 27 x cin: loaded but never stored
-        a_off[grp] = tap_offset(g, tap);
-        a_pl[grp] = ch;
+    // load warp: lane 0 waits and arms the barrier; lanes copy the 16 A groups and the
+    // cout/8 B planes of a stage in parallel
+    long long a_off = 0;
+    int a_pl = 0;
+    if (lane < 16) {  // source rows of A group `lane` (tap, 8-channel chunk) of this M tile
+      const int mg = mt * 128 + lane * 8;
+      int tap = mg / a.cin, ch = (mg % a.cin) / 8;
+      if (tap >= 27) tap = 0, ch = 0;  // rows beyond 27 x cin: loaded but never stored
+      a_off = tap_offset(g, tap);
+      a_pl = ch;
+    }
+    const int n_copies = 16 + a.cout / 8;
+    for (int st = 0; st < n_st; ++st) {
+      const int s = st % ns;
+      if (!umma::warp_wait(&empty[s], ((st / ns) & 1) ^ 1, WAIT_NS)) {
+        if (lane == 0) fail(ST_TIMEOUT_LOAD);
+        goto done;
       }
-      for (int st = 0; st < n_st; ++st) {
-        const int s = st % ns;
-        if (!mbar_wait_bounded(&empty[s], ((st / ns) & 1) ^ 1, WAIT_NS)) {
-          fail(ST_TIMEOUT_LOAD);
-          goto done;
-        }
-        mbar_arrive_expect_tx(&full[s], st_bytes);
-        const long long k0 = k_begin + (long long)st * WG_KT;
-        uint8_t* dst = sm + (size_t)s * st_bytes;
-        for (int grp = 0; grp < 16; ++grp)
-          umma::bulk_g2s(dst + grp * plane_tile, a.x + a_pl[grp] * a.plane + (g.margin + k0 + a_off[grp]) * 16,
-                         plane_tile, &full[s]);
-        for (int c = 0; c < a.cout / 8; ++c)
-          umma::bulk_g2s(dst + a_bytes + c * plane_tile, a.g + c * a.plane + (g.margin + k0) * 16, plane_tile,
+      if (lane == 0) mbar_arrive_expect_tx(&full[s], st_bytes);
+      __syncwarp();
+      const long long k0 = k_begin + (long long)st * WG_KT;
+      uint8_t* dst = sm + (size_t)s * st_bytes;
+      for (int c = lane; c < n_copies; c += 32) {
+        if (c < 16)
+          umma::bulk_g2s(dst + c * plane_tile, a.x + a_pl * a.plane + (g.margin + k0 + a_off) * 16, plane_tile,
                          &full[s]);
+        else
+          umma::bulk_g2s(dst + a_bytes + (c - 16) * plane_tile, a.g + (c - 16) * a.plane + (g.margin + k0) * 16,
+                         plane_tile, &full[s]);
       }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
-      const uint32_t idesc = umma::idesc_bf16(a.cout, true, true);
-      for (int st = 0; st < n_st; ++st) {
-        const int s = st % ns;
-        if (!mbar_wait_bounded(&full[s], (st / ns) & 1, WAIT_NS)) {
-          fail(ST_TIMEOUT_MMA);
-          goto done;
-        }
-        umma::fence_after_sync();
-        const uint32_t base = smem_u32(sm + (size_t)s * st_bytes);
-        for (int j = 0; j < WG_KT / 16; ++j) {
-          const uint64_t ad = umma::smem_desc(base + j * 256, 128, plane_tile);
-          const uint64_t bd = umma::smem_desc(base + a_bytes + j * 256, 128, plane_tile);
-          umma::mma_bf16(tmem, ad, bd, idesc, (st | j) != 0);
-        }
-        umma::commit(&empty[s]);
+    // MMA warp: whole warp walks the loop, one elected lane issues
+    const uint32_t idesc = umma::idesc_bf16(a.cout, true, true);
+    for (int st = 0; st < n_st; ++st) {
+      const int s = st % ns;
+      if (!umma::warp_wait(&full[s], (st / ns) & 1, WAIT_NS)) {
+        if (lane == 0) fail(ST_TIMEOUT_MMA);
+        goto done;
       }
-      if (n_st > 0) umma::commit(acc_full);
+      umma::fence_after_sync();
+      const uint32_t base = smem_u32(sm + (size_t)s * st_bytes);
+      uint64_t ad = umma::smem_desc(base, 128, plane_tile);
+      uint64_t bd = umma::smem_desc(base + a_bytes, 128, plane_tile);
+      for (int j = 0; j < WG_KT / 16; ++j, ad += 16, bd += 16)  // +256 bytes (16 rows) per K step
+        umma::mma_bf16_elect(tmem, ad, bd, idesc, (st | j) != 0);
+      umma::commit_elect(&empty[s]);
     }
+    if (n_st > 0) umma::commit_elect(acc_full);
   } else {
     const int q = warp & 3;
     const int r = 32 * q + lane;
@@ -472,6 +476,7 @@ __device__ __forceinline__ long long row_of(const Geo& g, int z, int y, int x) {
 struct InputArgs {
   const float* vol[4];
   float scale[4];
+  const float* scale_d;  // device scales (n_in floats) overriding scale[], or null
   int mode[4];
   int n_in, origin[3], vdim[3];
   uint8_t* x;
@@ -491,7 +496,8 @@ __global__ void k_pack_input(const InputArgs a) {
 #pragma unroll
   for (int c = 0; c < 16; ++c) f[c] = 0.f;
   for (int c = 0; c < a.n_in; ++c) {
-    float v = inside ? a.vol[c][src] * a.scale[c] : 0.f;
+    const float sc = a.scale_d ? a.scale_d[c] : a.scale[c];
+    float v = inside ? a.vol[c][src] * sc : 0.f;
     if (a.mode[c] == 1) v = sqrtf(fmaxf(v, 0.f));
     else if (a.mode[c] == 2) v = log1pf(fmaxf(v, 0.f));
     f[c] = v;
@@ -760,6 +766,13 @@ __global__ void k_input_maxima(const float* __restrict__ act, const float* __res
   }
 }
 
+// out[2..4] = network input scales from the maxima in out[0..1]: 1/max activity, 1, 1/max dose
+__global__ void k_input_scales(float* out) {
+  out[2] = out[0] > 0.f ? 1.f / out[0] : 0.f;
+  out[3] = 1.f;
+  out[4] = out[1] > 0.f ? 1.f / out[1] : 0.f;
+}
+
 // Adam with decoupled weight decay on FP32 parameters
 __global__ void k_adam(float* __restrict__ p, const float* __restrict__ gr, float* __restrict__ m,
                        float* __restrict__ v, long long n, float lr, float b1, float b2, float eps, float wd,
@@ -979,11 +992,11 @@ extern "C" pvd_status pvd_unet_pack_weights(const float* w, int cin, int cout, v
 }
 
 extern "C" pvd_status pvd_unet_pack_input(const pvd_unet_geom* geom, const float* const* volumes, const float* scales,
-                                          const int* modes, int n_in, const int* vol_dims, const int* origin, void* x,
-                                          pvd_stream stream) {
+                                          const float* scales_d, const int* modes, int n_in, const int* vol_dims,
+                                          const int* origin, void* x, pvd_stream stream) {
   pvd_status st = geo_check(geom);
   if (st != PVD_OK) return st;
-  if (n_in < 1 || n_in > 4 || !volumes || !scales || !modes || !vol_dims || !origin || !x || !al16(x))
+  if (n_in < 1 || n_in > 4 || !volumes || (!scales && !scales_d) || !modes || !vol_dims || !origin || !x || !al16(x))
     return set_error(PVD_ERR_ARG, "pvd_unet_pack_input: bad arguments");
   InputArgs a;
   a.g = make_geo(geom);
@@ -994,12 +1007,13 @@ extern "C" pvd_status pvd_unet_pack_input(const pvd_unet_geom* geom, const float
   }
   for (int c = 0; c < 4; ++c) {
     a.vol[c] = c < n_in ? volumes[c] : nullptr;
-    a.scale[c] = c < n_in ? scales[c] : 0.f;
+    a.scale[c] = (c < n_in && scales) ? scales[c] : 0.f;
     a.mode[c] = c < n_in ? modes[c] : 0;
     if (c < n_in && (!volumes[c] || modes[c] < 0 || modes[c] > 2))
       return set_error(PVD_ERR_ARG, "pvd_unet_pack_input: null volume or unknown mode");
   }
   a.n_in = n_in;
+  a.scale_d = scales_d;
   a.x = (uint8_t*)x;
   a.plane = a.g.rows * 16;
   const long long n = (long long)a.g.D * a.g.H * a.g.W;
@@ -1171,10 +1185,16 @@ extern "C" pvd_status pvd_unet_input_maxima(const float* activity, const float* 
                                             float rho_min, float* maxima, pvd_stream stream) {
   if (!activity || !density || !dose || !maxima || n < 0) return set_error(PVD_ERR_ARG, "pvd_unet_input_maxima: bad arguments");
   PVD_CUDA_TRY(cudaMemsetAsync(maxima, 0, 2 * sizeof(float), (cudaStream_t)stream));
-  if (n == 0) return PVD_OK;
+  if (n == 0) {
+    k_input_scales<<<1, 1, 0, (cudaStream_t)stream>>>(maxima);
+    PVD_LAUNCH_CHECK("k_input_scales");
+    return PVD_OK;
+  }
   const unsigned grid = (unsigned)std::min<long long>(blocks_for(n, 256), 4LL * sm_count());
   k_input_maxima<<<grid, 256, 0, (cudaStream_t)stream>>>(activity, density, dose, n, rho_min, maxima);
   PVD_LAUNCH_CHECK("k_input_maxima");
+  k_input_scales<<<1, 1, 0, (cudaStream_t)stream>>>(maxima);
+  PVD_LAUNCH_CHECK("k_input_scales");
   return PVD_OK;
 }
 

@@ -27,6 +27,7 @@ def test_trained_network_beats_plain_convolution():
     for p in held:
         corrected, fb = lc.predict(net, p.activity, p.density, p.dose_conv, sigma_max=float("inf"),
                                    return_fallback=True)
+        net.status()
         mc = p.dose_mc.cpu().numpy()
         rho = p.density.cpu().numpy()
         plain = lc.dose_errors(p.dose_conv.cpu().numpy(), mc, density=rho)
