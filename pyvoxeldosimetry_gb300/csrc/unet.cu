@@ -68,10 +68,18 @@ static Geo make_geo(const pvd_unet_geom* g) {
 
 __device__ __forceinline__ bool interior(const Geo& g, long long p) {
   if (p >= g.np) return false;
-  int x = (int)(p % g.Wp);
-  long long t = p / g.Wp;
-  int y = (int)(t % g.Hp);
-  int z = (int)(t / g.Hp);
+  int x, y, z;
+  if (g.np < (1LL << 31)) {  // 32-bit division (the 64-bit one is emulated and slow)
+    const uint32_t q = (uint32_t)p, t = q / (uint32_t)g.Wp;
+    x = (int)(q - t * (uint32_t)g.Wp);
+    z = (int)(t / (uint32_t)g.Hp);
+    y = (int)(t - (uint32_t)z * (uint32_t)g.Hp);
+  } else {
+    x = (int)(p % g.Wp);
+    const long long t = p / g.Wp;
+    y = (int)(t % g.Hp);
+    z = (int)(t / g.Hp);
+  }
   return x >= 1 && x <= g.W && y >= 1 && y <= g.H && z >= 1 && z <= g.D;
 }
 
