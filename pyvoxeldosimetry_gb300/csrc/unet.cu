@@ -318,6 +318,211 @@ done:
 }
 
 // ---------------------------------------------------------------------------
+// 3x3x3 convolution with the three dx taps stacked along N (for 16 or 32 output
+// channels, where an MMA costs the same ~40 cycles whatever its N up to 64):
+// for each (dz, dy) and 16 input channels, one MMA of 128 unshifted slab rows x
+// (3 x cout) columns gives P[r][dx][n]; the output row r of the tile is
+// P[r][0] + P[r+1][1] + P[r+2][2], summed by the epilogue through shared memory.
+// A tile therefore yields 126 output rows; 9 x cin/16 MMAs per tile instead of 27 x cin/16.
+// ---------------------------------------------------------------------------
+constexpr int STK_ROWS = 128;                      // slab rows = MMA rows
+constexpr int STK_OUT = STK_ROWS - 2;              // output rows per tile
+constexpr uint32_t STK_PITCH = STK_ROWS * 16;      // bytes of one plane's slab
+
+template <int CO>
+__global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3s(const ConvArgs a) {
+  extern __shared__ __align__(128) uint8_t sm[];
+  const int cin8 = a.cin >> 3;
+  constexpr int n3 = 3 * CO;
+  const uint32_t a_bytes = (uint32_t)cin8 * STK_PITCH;
+  const uint32_t g_bytes = (uint32_t)a.cin * n3 * 2;  // one (dz, dy) group's weights
+  const int na = a.na;
+  uint8_t* sa = sm;
+  uint8_t* sb = sm + (size_t)na * a_bytes;
+  constexpr int xp = CO + 1;  // exchange row pitch (odd: no bank conflicts)
+  float* xch = reinterpret_cast<float*>(sb + (size_t)9 * g_bytes);  // [2][128][cout + 1] exchange
+  uint64_t* full_a = reinterpret_cast<uint64_t*>(xch + 2 * STK_ROWS * xp);
+  uint64_t* empty_a = full_a + na;
+  uint64_t* full_w = empty_a + na;
+  uint64_t* acc_full = full_w + 1;
+  uint64_t* acc_empty = acc_full + 2;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);  // an epilogue warp timed out
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t ncols = umma::tmem_cols(2 * n3);
+
+  if (threadIdx.x == 0) {
+    *abort_flag = 0;
+    for (int i = 0; i < na; ++i) {
+      mbar_init(&full_a[i], 1);
+      mbar_init(&empty_a[i], 1);
+    }
+    mbar_init(full_w, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&acc_full[i], 1);
+      mbar_init(&acc_empty[i], 128);
+    }
+    fence_mbar_init();
+  }
+  if (warp == 1) umma::tmem_alloc(tslot, ncols);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *tslot;
+  const Geo& g = a.g;
+
+  if (warp == 0) {
+    // load warp: all 9 groups' weights once (lanes 0-8), then the slabs (lane c: plane c)
+    if (lane == 0) mbar_arrive_expect_tx(full_w, 9 * g_bytes);
+    __syncwarp();
+    if (lane < 9) umma::bulk_g2s(sb + (size_t)lane * g_bytes, a.w + (size_t)lane * g_bytes, g_bytes, full_w);
+    int it_a = 0;
+    for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x) {
+      const long long p0 = (long long)tile * STK_OUT;
+      for (int grp = 0; grp < 9; ++grp) {
+        const int dz = grp / 3, dy = grp % 3;
+        const long long row0 = g.margin + p0 + (long long)(dz - 1) * g.Hp * g.Wp + (long long)(dy - 1) * g.Wp - 1;
+        const int s = it_a % na;
+        if (!umma::warp_wait(&empty_a[s], ((it_a / na) & 1) ^ 1, WAIT_NS)) {
+          if (lane == 0) fail(ST_TIMEOUT_LOAD);
+          goto done;
+        }
+        if (lane == 0) mbar_arrive_expect_tx(&full_a[s], a_bytes);
+        __syncwarp();
+        for (int c = lane; c < cin8; c += 32)
+          umma::bulk_g2s(sa + (size_t)s * a_bytes + (size_t)c * STK_PITCH, a.x + c * a.plane + row0 * 16, STK_PITCH,
+                         &full_a[s]);
+        ++it_a;
+      }
+    }
+  } else if (warp == 1) {
+    const uint32_t idesc = umma::idesc_bf16(n3, false, false);
+    const uint32_t b_lbo = (uint32_t)n3 * 16;
+    const uint64_t a_kstep = (2 * STK_PITCH) >> 4;
+    const uint64_t b_kstep = (2 * b_lbo) >> 4;
+    const int ksteps = a.cin / 16;
+    int it_a = 0, t_local = 0;
+    if (!umma::warp_wait(full_w, 0, WAIT_NS)) {
+      if (lane == 0) fail(ST_TIMEOUT_MMA);
+      goto done;
+    }
+    for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++t_local) {
+      const int acc = t_local & 1;
+      if (!umma::warp_wait(&acc_empty[acc], ((t_local >> 1) & 1) ^ 1, WAIT_NS)) {
+        if (lane == 0) fail(ST_TIMEOUT_MMA);
+        goto done;
+      }
+      umma::fence_after_sync();
+      const uint32_t d = tmem + (uint32_t)(acc * n3);
+      for (int grp = 0; grp < 9; ++grp) {
+        const int s = it_a % na;
+        if (!umma::warp_wait(&full_a[s], (it_a / na) & 1, WAIT_NS)) {
+          if (lane == 0) fail(ST_TIMEOUT_MMA);
+          goto done;
+        }
+        umma::fence_after_sync();
+        uint64_t ad = umma::smem_desc(smem_u32(sa + (size_t)s * a_bytes), STK_PITCH, 128);
+        uint64_t bd = umma::smem_desc(smem_u32(sb + (size_t)grp * g_bytes), b_lbo, 128);
+        for (int kc = 0; kc < ksteps; ++kc, ad += a_kstep, bd += b_kstep)
+          umma::mma_bf16_elect(d, ad, bd, idesc, (grp | kc) != 0);
+        umma::commit_elect(&empty_a[s]);
+        ++it_a;
+      }
+      umma::commit_elect(&acc_full[acc]);
+    }
+  } else {
+    // epilogue: thread r holds P[r][dx][n]; it publishes P[r][1] and P[r][2], then
+    // sums P[r][0] + P[r+1][1] + P[r+2][2] for output row p0 + r (r < 126).  The four
+    // warps meet at named barriers; a warp whose wait timed out still takes part and
+    // raises the abort flag, so all four leave the loop together.
+    const int q = warp & 3;
+    const int r = 32 * q + lane;
+    constexpr int co = CO;
+    float* x1 = xch;                 // [128][cout + 1]: P[.][1]
+    float* x2 = xch + STK_ROWS * xp; // [128][cout + 1]: P[.][2]
+    int t_local = 0;
+    for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++t_local) {
+      const int acc = t_local & 1;
+      const bool ok = umma::warp_wait(&acc_full[acc], (t_local >> 1) & 1, WAIT_NS);
+      float v0[CO];
+      if (ok) {
+        umma::fence_after_sync();
+        const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * n3);
+#pragma unroll
+        for (int c0 = 0; c0 < co; c0 += 16) {
+          float t[16];
+          umma::tmem_ld16(trow + (uint32_t)c0, t);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v0[c0 + j] = t[j];
+          umma::tmem_ld16(trow + (uint32_t)(co + c0), t);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) x1[r * xp + c0 + j] = t[j];
+          umma::tmem_ld16(trow + (uint32_t)(2 * co + c0), t);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) x2[r * xp + c0 + j] = t[j];
+        }
+        umma::fence_before_sync();
+        umma::mbar_arrive(&acc_empty[acc]);  // TMEM read: the MMA warp may reuse it
+      } else if (lane == 0) {
+        fail(ST_TIMEOUT_EPI);
+        *abort_flag = 1;
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");
+      const bool stop = *abort_flag != 0;
+      const long long p = (long long)tile * STK_OUT + r;
+      if (!stop && r < STK_OUT && p < g.np) {
+        const bool in = interior(g, p);
+        const long long roff = (g.margin + p) * 16;
+#pragma unroll
+        for (int c0 = 0; c0 < co; c0 += 16) {
+          float v[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = v0[c0 + j] + x1[(r + 1) * xp + c0 + j] + x2[(r + 2) * xp + c0 + j];
+          if (a.bias) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] += __ldg(a.bias + c0 + j);
+          }
+          if (a.flags & PVD_UNET_ACT_LEAKY) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = v[j] > 0.f ? v[j] : v[j] * a.slope;
+          }
+          const int pl = c0 >> 3;
+          if (in && a.mask) {
+            float m[16];
+            unpack8(*reinterpret_cast<const uint4*>(a.mask + pl * a.plane + roff), m);
+            unpack8(*reinterpret_cast<const uint4*>(a.mask + (pl + 1) * a.plane + roff), m + 8);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] *= leaky_grad(m[j], a.slope);
+          }
+          if (in && (a.flags & PVD_UNET_ACCUMULATE)) {
+            float o[16];
+            unpack8(*reinterpret_cast<const uint4*>(a.y + pl * a.plane + roff), o);
+            unpack8(*reinterpret_cast<const uint4*>(a.y + (pl + 1) * a.plane + roff), o + 8);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] += o[j];
+          }
+          if (!in) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = 0.f;
+          }
+          *reinterpret_cast<uint4*>(a.y + pl * a.plane + roff) = pack8(v);
+          *reinterpret_cast<uint4*>(a.y + (pl + 1) * a.plane + roff) = pack8(v + 8);
+        }
+      }
+      asm volatile("bar.sync 1, 128;" ::: "memory");  // exchange buffer free for the next tile
+      if (stop) break;
+    }
+  }
+done:
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 1) {
+    umma::fence_after_sync();
+    umma::tmem_dealloc(tmem, ncols);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // weight gradient: partial[split][mt][m][n] = sum over this split's rows
 // ---------------------------------------------------------------------------
 struct WgradArgs {
@@ -462,14 +667,24 @@ __global__ void k_wgrad_reduce(const float* __restrict__ partial, float* __restr
 // weight packing: FP32 [cout][cin][27] -> BF16 forward [27][cin/8][cout][8] and
 // data-gradient [27][cout/8][cin][8] with the taps mirrored
 // ---------------------------------------------------------------------------
+// index of element (tap t, K channel kk, N channel nn) of a packed weight buffer for a
+// convolution kernel with CI input and CO output channels: per-tap layout
+// [27][CI/8][CO][8], or dx-stacked layout [9 (dz,dy)][CI/8][3 dx x CO][8]
+__device__ __forceinline__ size_t packed_index(int t, int kk, int nn, int CI, int CO, bool stacked) {
+  if (!stacked) return (((size_t)t * (CI / 8) + kk / 8) * CO + nn) * 8 + (kk % 8);
+  return (((size_t)(t / 3) * (CI / 8) + kk / 8) * (3 * CO) + (t % 3) * CO + nn) * 8 + (kk % 8);
+}
+
+// FP32 [cout][cin][27] -> BF16 forward weights (kernel cin -> cout) and data-gradient
+// weights (kernel cout -> cin, taps mirrored)
 __global__ void k_pack_weights(const float* __restrict__ w, int cin, int cout, __nv_bfloat16* fwd,
-                               __nv_bfloat16* bwd) {
+                               __nv_bfloat16* bwd, int fwd_stacked, int bwd_stacked) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cout * cin * 27) return;
   const int tap = i % 27, k = (i / 27) % cin, n = i / (27 * cin);
   const __nv_bfloat16 v = __float2bfloat16_rn(w[i]);
-  if (fwd) fwd[(((size_t)tap * (cin / 8) + k / 8) * cout + n) * 8 + (k % 8)] = v;
-  if (bwd) bwd[(((size_t)(26 - tap) * (cout / 8) + n / 8) * cin + k) * 8 + (n % 8)] = v;
+  if (fwd) fwd[packed_index(tap, k, n, cin, cout, fwd_stacked)] = v;
+  if (bwd) bwd[packed_index(26 - tap, n, k, cout, cin, bwd_stacked)] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -821,22 +1036,38 @@ static size_t conv_smem(int cin, int cout, int na, int nb) {
 struct ConvPlanSm {
   int na, nb, resident, occ;
   size_t smem;
+  int stacked;  // dx taps stacked along N (k_conv3s)
 };
 
+static size_t conv_smem_stacked(int cin, int cout, int na) {
+  return (size_t)na * (cin / 8) * STK_PITCH + (size_t)27 * cin * cout * 2 + (size_t)2 * STK_ROWS * (cout + 1) * 4 +
+         (size_t)(2 * na + 5) * 8 + 4 + 16;
+}
+
 static ConvPlanSm conv_plan(int cin, int cout) {
-  ConvPlanSm p{0, 0, 0, 0, 0};
+  ConvPlanSm p{0, 0, 0, 0, 0, 0};
+  // 16 or 32 output channels: dx taps stacked along N, weights resident, the deepest
+  // slab ring that lets 4, else 2, else 1 CTAs share an SM
+  if (cout == 16 || cout == 32) {
+    for (int target : {4, 2, 1}) {
+      const size_t budget = std::min((size_t)MAX_SMEM, (size_t)(233472 / target) - 2048);
+      for (int na = 9; na >= 2 && !p.na; --na)
+        if (conv_smem_stacked(cin, cout, na) <= budget) p = {na, 0, 1, 0, conv_smem_stacked(cin, cout, na), 1};
+      if (p.na) return p;
+    }
+  }
   // resident weights: the deepest input-slab ring (up to a whole tile's 9 slabs) that
   // still lets 4, else 2, else 1 CTAs share an SM
   for (int target : {4, 2, 1}) {
     const size_t budget = std::min((size_t)MAX_SMEM, (size_t)(233472 / target) - 2048);
     for (int na = 9; na >= 2 && !p.na; --na)
-      if (conv_smem(cin, cout, na, 27) <= budget) p = {na, 27, 1, 0, conv_smem(cin, cout, na, 27)};
+      if (conv_smem(cin, cout, na, 27) <= budget) p = {na, 27, 1, 0, conv_smem(cin, cout, na, 27), 0};
     if (p.na) break;
   }
   if (!p.na) {
     int nb = 4;
     while (nb > 2 && conv_smem(cin, cout, 2, nb) > (size_t)MAX_SMEM) --nb;
-    p = {2, nb, 0, 0, conv_smem(cin, cout, 2, nb)};
+    p = {2, nb, 0, 0, conv_smem(cin, cout, 2, nb), 0};
   }
   return p;
 }
@@ -868,9 +1099,17 @@ extern "C" pvd_status pvd_unet_geometry(int d, int h, int w, pvd_unet_geom* out)
   out->dims[2] = w;
   out->padded = dp * hp * wp;
   out->padded_tiles = (out->padded + TILE_M - 1) / TILE_M * TILE_M;
-  out->margin = (hp * wp + wp + 2 + 7) / 8 * 8;
+  // zero rows either side: the largest tap offset plus one 128-row tile, so every
+  // slab a convolution tile reads lies inside the plane
+  out->margin = (hp * wp + wp + 2 + 7) / 8 * 8 + TILE_M;
   out->rows = out->margin + out->padded_tiles + out->margin;
   return PVD_OK;
+}
+
+// the kernel a plan launches
+static const void* conv_kernel(const ConvPlanSm& pl, int cout) {
+  if (!pl.stacked) return (const void*)k_conv3;
+  return cout == 16 ? (const void*)k_conv3s<16> : (const void*)k_conv3s<32>;
 }
 
 extern "C" pvd_status pvd_unet_conv3d(const pvd_unet_geom* geom, const void* x, int cin, const void* w_packed,
@@ -887,26 +1126,28 @@ extern "C" pvd_status pvd_unet_conv3d(const pvd_unet_geom* geom, const void* x, 
   static bool have[17][17];
   ConvPlanSm& pl = plans[cin / 16][cout / 16];
   if (!have[cin / 16][cout / 16]) {
-    pl = conv_plan(cin, cout);
-    if (pl.smem > (size_t)MAX_SMEM)
+    ConvPlanSm np = conv_plan(cin, cout);
+    if (np.smem > (size_t)MAX_SMEM)
       return set_error(PVD_ERR_UNSUPPORTED, "pvd_unet_conv3d: channel counts need more shared memory than a CTA has");
-    PVD_CUDA_TRY(cudaFuncSetAttribute(k_conv3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MAX_SMEM));
+    const void* kern = conv_kernel(np, cout);
+    PVD_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MAX_SMEM));
     // CTAs that can be resident on one SM at once: registers (allocated per warp in
     // units of 256), shared memory (228 KB per SM, 1 KB reserved per CTA), threads,
-    // and TMEM (512 columns per SM; a CTA holds two accumulators of cout columns)
+    // and TMEM (512 columns per SM; a CTA holds two accumulators)
     cudaFuncAttributes fa;
-    PVD_CUDA_TRY(cudaFuncGetAttributes(&fa, k_conv3));
+    PVD_CUDA_TRY(cudaFuncGetAttributes(&fa, kern));
     const int regs_warp = (fa.numRegs * 32 + 255) / 256 * 256;
     const int by_regs = 65536 / (regs_warp * (CONV_THREADS / 32));
-    const int by_smem = (int)(233472 / (pl.smem + fa.sharedSizeBytes + 1024));
+    const int by_smem = (int)(233472 / (np.smem + fa.sharedSizeBytes + 1024));
     const int by_threads = 2048 / CONV_THREADS;
-    const int by_tmem = (int)(512 / umma::tmem_cols(2 * cout));
-    pl.occ = std::max(1, std::min(std::min(by_regs, by_smem), std::min(by_threads, by_tmem)));
+    const int by_tmem = (int)(512 / umma::tmem_cols(2 * cout * (np.stacked ? 3 : 1)));
+    np.occ = std::max(1, std::min(std::min(by_regs, by_smem), std::min(by_threads, by_tmem)));
     // when TMEM is the binding limit, request enough shared memory that no more CTAs
     // than that can be co-resident (an extra CTA would wait in tcgen05.alloc for a
     // persistent CTA to finish)
     if (by_tmem < std::min(std::min(by_regs, by_smem), by_threads))
-      pl.smem = std::max(pl.smem, (size_t)(233472 / by_tmem) - 1024 - fa.sharedSizeBytes);
+      np.smem = std::max(np.smem, (size_t)(233472 / by_tmem) - 1024 - fa.sharedSizeBytes);
+    pl = np;
     have[cin / 16][cout / 16] = true;
   }
   const size_t smem = pl.smem;
@@ -925,6 +1166,16 @@ extern "C" pvd_status pvd_unet_conv3d(const pvd_unet_geom* geom, const void* x, 
   a.slope = slope;
   a.g = make_geo(geom);
   a.plane = a.g.rows * 16;
+  if (pl.stacked) {
+    a.n_tiles = (int)((a.g.np + STK_OUT - 1) / STK_OUT);
+    const int grid = std::min(a.n_tiles, sm_count() * pl.occ);
+    if (cout == 16)
+      k_conv3s<16><<<grid, CONV_THREADS, smem, (cudaStream_t)stream>>>(a);
+    else
+      k_conv3s<32><<<grid, CONV_THREADS, smem, (cudaStream_t)stream>>>(a);
+    PVD_LAUNCH_CHECK("k_conv3s");
+    return PVD_OK;
+  }
   a.n_tiles = (int)(a.g.np_tiles / TILE_M);
   const int grid = std::min(a.n_tiles, sm_count() * pl.occ);
   k_conv3<<<grid, CONV_THREADS, smem, (cudaStream_t)stream>>>(a);
@@ -993,8 +1244,10 @@ extern "C" pvd_status pvd_unet_pack_weights(const float* w, int cin, int cout, v
   if (!w || (!fwd_packed && !bwd_packed) || !ch_ok(cin) || !ch_ok(cout))
     return set_error(PVD_ERR_ARG, "pvd_unet_pack_weights: bad arguments");
   const int total = cout * cin * 27;
+  // each buffer in the layout the convolution of those channels will read
+  const int fs = conv_plan(cin, cout).stacked, bs = conv_plan(cout, cin).stacked;
   k_pack_weights<<<blocks_for(total, 256), 256, 0, (cudaStream_t)stream>>>(w, cin, cout, (__nv_bfloat16*)fwd_packed,
-                                                                          (__nv_bfloat16*)bwd_packed);
+                                                                          (__nv_bfloat16*)bwd_packed, fs, bs);
   PVD_LAUNCH_CHECK("k_pack_weights");
   return PVD_OK;
 }

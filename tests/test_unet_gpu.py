@@ -95,11 +95,12 @@ def test_conv_forward(env, cin, cout):
     assert _halo_zero(y, lc)
 
 
-@pytest.mark.parametrize("cin,cout,mode", [(16, 16, "fwd"), (128, 128, "fwd"), (192, 64, "fwd"),
-                                            (96, 32, "dgrad"), (64, 192, "dgrad")])
+@pytest.mark.parametrize("cin,cout,mode", [(16, 16, "fwd"), (32, 32, "fwd"), (96, 32, "fwd"), (128, 128, "fwd"),
+                                            (192, 64, "fwd"), (96, 32, "dgrad"), (64, 192, "dgrad")])
 def test_conv_persistent_many_tiles(env, cin, cout, mode):
-    """1170 row tiles: more than one tile per persistent CTA, both weight modes
-    (all taps resident for the small layers, a ring of tap slots for the large)."""
+    """About 1170 row tiles: more than one tile per persistent CTA, all three kernel
+    forms (dx taps stacked along N for 16/32 output channels, all taps resident, a
+    ring of tap slots for the large layers)."""
     N, lc, lib, dev = env
     dims = (46, 50, 58)
     gen = torch.Generator().manual_seed(3 * cin + cout)
@@ -128,7 +129,7 @@ def test_conv_persistent_many_tiles(env, cin, cout, mode):
     assert _halo_zero(y, lc)
 
 
-@pytest.mark.parametrize("cin,cout", [(16, 16), (48, 16), (96, 32), (192, 64), (128, 128)])
+@pytest.mark.parametrize("cin,cout", [(16, 16), (32, 64), (48, 16), (96, 32), (192, 64), (128, 128)])
 def test_conv_data_gradient(env, cin, cout):
     """Input gradient of a cin -> cout conv: the kernel run cout -> cin on the
     mirrored packing, times leaky'(mask), then with accumulation."""
