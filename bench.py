@@ -492,6 +492,7 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
     plan.close()
     conv.close()
     net.status()
+    large = None if small else measure_unet_large(device, net)
     st = np.stack(batches)
     mean = st.mean(0)
     sel = mean > 0.1 * mean.max()
@@ -511,21 +512,66 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
         "tensor_peak_tflops": tc_peak, "tensor_peak_source": tc_src,
         "mc_histories_per_batch": hb, "mc_ms_10_batches": mc_ms, "mc_median_rel_se": rse_med,
         "mc_to_1pct_ms": mc_1pct_ms, "nn_vs_mc_1pct_speedup": mc_1pct_ms / nn_ms,
+        "whole_body_512x512x400": large,
     }
+
+
+def measure_unet_large(device, net, reps=2):
+    """NN-corrected dose of one whole-body 512x512x400 volume at 1.5 mm (the survey's
+    inference size): plain density-scaled Y-90 convolution + U-Net + apply, CUDA events
+    around each call, inputs resident."""
+    import torch
+    from pyvoxeldosimetry_gb300 import phantoms
+    from pyvoxeldosimetry_gb300.core import learned_correction as lc
+    from pyvoxeldosimetry_gb300.core.kernel_convolution import KernelConvolutionCalculator
+    shape, vox = (400, 512, 512), (1.5, 1.5, 1.5)
+    act, rho = phantoms.ct_phantom(shape, 1.5, seed=11)
+    a = torch.from_numpy(act).to(device)
+    r = torch.from_numpy(rho).to(device)
+    del act, rho
+    conv = KernelConvolutionCalculator("Y90")
+    out = torch.empty(shape, dtype=torch.float32, device=device)
+    d = conv.calculate_dose_rate(a, vox, density=r)
+    lc.predict(net, a, r, d, out=out)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    conv_ms, inf_ms = [], []
+    for _ in range(reps):
+        e0.record()
+        d = conv.calculate_dose_rate(a, vox, density=r)
+        e1.record()
+        e1.synchronize()
+        conv_ms.append(e0.elapsed_time(e1))
+        e0.record()
+        lc.predict(net, a, r, d, out=out)
+        e1.record()
+        e1.synchronize()
+        inf_ms.append(e0.elapsed_time(e1))
+    net.status()
+    conv.close()
+    c, i = float(np.median(conv_ms)), float(np.median(inf_ms))
+    nvox = float(np.prod(shape))
+    res = {"shape": list(shape), "plain_conv_ms": c, "unet_inference_ms": i, "nn_corrected_ms": c + i,
+           "nn_corrected_gvox_s": nvox / ((c + i) / 1e3) / 1e9,
+           "unet_inference_tflops": lc.conv_flops(shape) / (i / 1e3) / 1e12,
+           "device_memory_peak_gb": torch.cuda.max_memory_allocated(device) / 1e9}
+    net._ws.clear()
+    del a, r, d, out
+    torch.cuda.empty_cache()
+    return res
 
 
 def measure_unet_accuracy(device, small=False):
     """What the learned correction gains, measured in the same run: the U-Net trained
     on this package's own pairs (seeded 48^3 CT-like phantoms at 4 mm, Y-90, density-
-    scaled convolution vs GPU Monte Carlo with 2e7 histories), judged on two held-out
-    phantoms against Monte Carlo with 1e8 histories, tissue voxels above 10 % of the
+    scaled convolution vs GPU Monte Carlo with 1e8 histories), judged on two held-out
+    phantoms against Monte Carlo with 2e8 histories, tissue voxels above 10 % of the
     tissue maximum: relative error of the plain and of the corrected dose."""
     from pyvoxeldosimetry_gb300.core import learned_correction as lc
     shape, vox = (48, 48, 48), 4.0
-    n_train, steps = (4, 300) if small else (12, 1500)
+    n_train, steps, hist = (4, 300, 20_000_000) if small else (24, 5000, 100_000_000)
     t0 = time.perf_counter()
-    pairs = lc.generate_training_pairs(n_train, shape, vox, "Y90", histories=20_000_000, seed=100, device=device)
-    held = lc.generate_training_pairs(2, shape, vox, "Y90", histories=100_000_000, seed=900, device=device)
+    pairs = lc.generate_training_pairs(n_train, shape, vox, "Y90", histories=hist, seed=100, device=device)
+    held = lc.generate_training_pairs(2, shape, vox, "Y90", histories=200_000_000, seed=900, device=device)
     net = lc.UNet3D(seed=0, device=device)
     st = lc.train(net, pairs, steps, crop=shape, lr=1e-3)
     res = {"plain": [], "corrected": []}
@@ -540,8 +586,9 @@ def measure_unet_accuracy(device, small=False):
     return {"train_steps": steps, "train_phantoms": n_train, "train_seconds": st.seconds,
             "total_seconds": time.perf_counter() - t0, "held_out_phantoms": len(held),
             "plain_vs_mc": agg["plain"], "corrected_vs_mc": agg["corrected"],
+            "histories_per_training_phantom": hist,
             "judged": "tissue voxels (density >= 0.2) above 10 % of the tissue maximum; relative error to "
-                      "MC with 1e8 histories"}
+                      "MC with 2e8 histories"}
 
 
 def run_only(args, device):
