@@ -525,9 +525,13 @@ pvd_status pvd_unet_conv3d_wgrad(const pvd_unet_geom* geom, const void* x, int c
                                  float* dw, int accumulate, void* workspace, size_t workspace_bytes,
                                  pvd_stream stream);
 
-/* FP32 weights [cout][cin][27] -> BF16 forward layout [27][cin/8][cout][8]
- * (fwd_packed) and data-gradient layout [27][cout/8][cin][8] with mirrored
- * taps (bwd_packed); either output may be NULL. */
+/* FP32 weights [cout][cin][27] -> BF16 packed weights (27 * cin * cout values
+ * each) for the forward convolution cin -> cout (fwd_packed) and for the data
+ * gradient cout -> cin with mirrored taps (bwd_packed); either output may be
+ * NULL.  The packed layout is internal to this library and chosen per channel
+ * pair the way pvd_unet_conv3d chooses its kernel: per tap [27][K/8][N][8], or,
+ * for 16 or 32 output channels, with the three x taps stacked along N
+ * [9][K/8][3N][8]. */
 pvd_status pvd_unet_pack_weights(const float* w, int cin, int cout, void* fwd_packed, void* bwd_packed,
                                  pvd_stream stream);
 

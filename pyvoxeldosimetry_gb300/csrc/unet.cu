@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "pvd_common.cuh"
@@ -1124,7 +1125,8 @@ extern "C" pvd_status pvd_unet_conv3d(const pvd_unet_geom* geom, const void* x, 
   // launch configuration per (cin, cout), computed once per process (one device)
   static ConvPlanSm plans[17][17];
   static bool have[17][17];
-  ConvPlanSm& pl = plans[cin / 16][cout / 16];
+  static std::mutex plans_mu;
+  std::unique_lock<std::mutex> lock(plans_mu);
   if (!have[cin / 16][cout / 16]) {
     ConvPlanSm np = conv_plan(cin, cout);
     if (np.smem > (size_t)MAX_SMEM)
@@ -1147,9 +1149,11 @@ extern "C" pvd_status pvd_unet_conv3d(const pvd_unet_geom* geom, const void* x, 
     // persistent CTA to finish)
     if (by_tmem < std::min(std::min(by_regs, by_smem), by_threads))
       np.smem = std::max(np.smem, (size_t)(233472 / by_tmem) - 1024 - fa.sharedSizeBytes);
-    pl = np;
+    plans[cin / 16][cout / 16] = np;
     have[cin / 16][cout / 16] = true;
   }
+  const ConvPlanSm pl = plans[cin / 16][cout / 16];
+  lock.unlock();
   const size_t smem = pl.smem;
   ConvArgs a;
   a.x = (const uint8_t*)x;
