@@ -94,3 +94,20 @@ def test_validation_before_any_cuda_call():
     # Adam needs step >= 1
     assert lib.pvd_adam_step(fake, fake, fake, fake, 10, 1e-3, 0.9, 0.999, 1e-8, 0.0, 0, None) == 1
     assert "pvd_adam_step" in N.last_error()
+
+
+def test_nn_corrected_calculator_needs_a_model():
+    from pyvoxeldosimetry_gb300 import DoseCalculator, NNCorrectedDoseCalculator
+    with pytest.raises(ValueError):
+        DoseCalculator("Y90", method="nn_corrected")
+    with pytest.raises(TypeError):
+        NNCorrectedDoseCalculator(["Y90", "Lu177"], config={"model_path": "x.npz"})
+
+
+def test_dose_errors_restricts_to_tissue_above_threshold():
+    d = np.array([1.0, 2.0, 3.0, 10.0, 0.5])
+    ref = np.array([1.0, 2.2, 3.0, 10.0, 0.5])
+    rho = np.array([1.0, 1.0, 0.01, 1.0, 1.0])  # voxel 2 is air
+    e = lc.dose_errors(d, ref, rel_threshold=0.1, density=rho)
+    assert e["voxels"] == 2  # 2.2 and 10.0: strictly above 10 % of the tissue max 10; 3.0 is air
+    assert e["max"] == pytest.approx(0.2 / 2.2)
