@@ -517,7 +517,7 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
 
 
 def measure_unet_large(device, net, reps=2):
-    """NN-corrected dose of one whole-body 512x512x400 volume at 1.5 mm (the survey's
+    """NN-corrected dose of one whole-body 512x512x400 volume at 1.5 mm (the whole-body
     inference size): plain density-scaled Y-90 convolution + U-Net + apply, CUDA events
     around each call, inputs resident."""
     import torch
