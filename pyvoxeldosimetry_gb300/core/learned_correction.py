@@ -396,24 +396,32 @@ def _input_scales_device(activity: torch.Tensor, density: torch.Tensor, dose: to
     return mx[2:5]
 
 
-def make_pair(activity: np.ndarray, density: np.ndarray, dose_conv: np.ndarray, dose_mc: np.ndarray,
-              rel_threshold: float = 0.1, device=None) -> TrainingPair:
-    """Target log ratio and weight (host arithmetic on one phantom's doses: data
-    preparation, not the dose path).  Weighted voxels: tissue (density >=
-    TISSUE_DENSITY) whose convolution dose exceeds rel_threshold x its maximum
-    over tissue.  Air is excluded because dose to local mass there is dominated
-    by the 1000x smaller mass, in both methods."""
+def log_ratio_target(dose_conv: np.ndarray, dose_mc: np.ndarray, density: np.ndarray,
+                     rel_threshold: float = 0.1) -> Tuple[np.ndarray, np.ndarray, float]:
+    """Training target and weight of one phantom (host arithmetic: data preparation,
+    not the dose path).  Weighted voxels: tissue (density >= TISSUE_DENSITY) whose
+    convolution dose exceeds rel_threshold x its maximum over tissue, with both doses
+    positive; target log(D_MC / D_conv) clipped to [-3, 3] there, 0 elsewhere.  Air is
+    excluded because dose to local mass there is dominated by the 1000x smaller mass,
+    in both methods.  Returns (target float32, weight float32, tissue dose maximum)."""
     dc = np.asarray(dose_conv, np.float64)
     dm = np.asarray(dose_mc, np.float64)
     tissue = np.asarray(density) >= TISSUE_DENSITY
-    thr = rel_threshold * (dc[tissue].max() if tissue.any() else 0.0)
-    ok = tissue & (dc > thr) & (dm > 0) & (dc > 0)
+    dmax = float(dc[tissue].max()) if tissue.any() else float(dc.max())
+    ok = tissue & (dc > rel_threshold * dmax) & (dm > 0) & (dc > 0)
     tgt = np.zeros(dc.shape, np.float32)
     tgt[ok] = np.clip(np.log(dm[ok] / dc[ok]), -3.0, 3.0)
+    return tgt, ok.astype(np.float32), dmax
+
+
+def make_pair(activity: np.ndarray, density: np.ndarray, dose_conv: np.ndarray, dose_mc: np.ndarray,
+              rel_threshold: float = 0.1, device=None) -> TrainingPair:
+    """One phantom's volumes on the device, with its target and weight (``log_ratio_target``)."""
+    tgt, w, dmax = log_ratio_target(dose_conv, dose_mc, density, rel_threshold)
     dev = _require_cuda(device)
     T = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(dev)  # noqa: E731
-    return TrainingPair(T(activity), T(density), T(dose_conv), T(dose_mc), T(tgt), T(ok.astype(np.float32)),
-                        input_scales(float(np.max(activity)), float(dc[tissue].max() if tissue.any() else dc.max())))
+    return TrainingPair(T(activity), T(density), T(dose_conv), T(dose_mc), T(tgt), T(w),
+                        input_scales(float(np.max(activity)), dmax))
 
 
 def generate_training_pairs(n: int, shape=(64, 64, 64), voxel_mm: float = 4.0, radionuclide: str = "Y90",

@@ -111,3 +111,16 @@ def test_dose_errors_restricts_to_tissue_above_threshold():
     e = lc.dose_errors(d, ref, rel_threshold=0.1, density=rho)
     assert e["voxels"] == 2  # 2.2 and 10.0: strictly above 10 % of the tissue max 10; 3.0 is air
     assert e["max"] == pytest.approx(0.2 / 2.2)
+
+
+def test_log_ratio_target():
+    dc = np.array([10.0, 5.0, 0.5, 8.0, 4.0, 100.0])
+    dm = np.array([12.0, 5.0, 0.6, 0.0, 4.0 * np.e ** 5, 1.0])
+    rho = np.array([1.0, 0.3, 1.0, 1.0, 1.85, 0.0012])  # last voxel is air
+    t, w, dmax = lc.log_ratio_target(dc, dm, rho, rel_threshold=0.1)
+    assert dmax == 10.0  # the air voxel's 100 is not a tissue maximum
+    # weighted: tissue, conv dose > 1.0, both doses positive
+    assert w.tolist() == [1.0, 1.0, 0.0, 0.0, 1.0, 0.0]
+    assert t[0] == pytest.approx(np.log(1.2)) and t[1] == 0.0
+    assert t[4] == pytest.approx(3.0)  # clipped
+    assert t.dtype == np.float32 and w.dtype == np.float32
