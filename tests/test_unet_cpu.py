@@ -124,3 +124,26 @@ def test_log_ratio_target():
     assert t[0] == pytest.approx(np.log(1.2)) and t[1] == 0.0
     assert t[4] == pytest.approx(3.0)  # clipped
     assert t.dtype == np.float32 and w.dtype == np.float32
+
+
+def test_every_bulk_copy_stays_inside_the_plane():
+    """Row ranges read by the tensor-core kernels' bulk copies, restated from their
+    tiling, against the plane size pvd_unet_geometry gives (random grids)."""
+    rng = np.random.default_rng(4)
+    for _ in range(300):
+        d, h, w = (int(v) for v in rng.integers(1, 90, 3))
+        g = lc.geometry((d, h, w))
+        hp, wp = h + 2, w + 2
+        reach = hp * wp + wp + 1  # largest |tap offset|
+        # k_conv3: tiles of 128 rows over padded_tiles; slab rows [p0 + off(dz,dy) - 1, +130)
+        last_p0 = g.padded_tiles - 128
+        assert g.margin - reach >= 0
+        assert g.margin + last_p0 + (hp * wp + wp) - 1 + 130 <= g.rows
+        # k_conv3s: tiles of 126 output rows over padded; slab rows [p0 + off(dz,dy) - 1, +128)
+        n_tiles = -(-g.padded // 126)
+        last_p0s = (n_tiles - 1) * 126
+        assert g.margin + last_p0s + (hp * wp + wp) - 1 + 128 <= g.rows
+        # k_wgrad: stages of 64 rows over padded_tiles, A rows shifted by any tap offset
+        assert g.margin + (g.padded_tiles - 64) + reach + 64 <= g.rows
+        # outputs: every written row p < padded_tiles lies inside the plane
+        assert g.margin + g.padded_tiles <= g.rows
