@@ -59,9 +59,13 @@ WORKLOADS = {
 }
 PASS_NAMES = ["x_fwd", "y_fwd", "z_fwd_mul_inv", "y_inv", "x_inv"]
 PASS_KERNELS = ["kf_x_fwd", "kf_y<0>", "kf_z", "kf_y<1>", "kf_x_inv"]
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch, from one ncu --set full capture
-# of the same bench command (profiles/kf_x_inv_ct256_y90_lu177_i131.md)
-NCU_DRAM_BYTES_PER_LAUNCH = {"ct256_y90_lu177_i131": {"kf_x_inv": 142_640_128 + 37_710_592}}
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of a kernel, from one ncu capture of
+# that kernel (one launch, --clock-control none) on this workload, keyed by workload, kernel and
+# FFT lengths: the figure is reported only when the run's dominant pass and lengths match the key
+# (null otherwise), so a changed kernel or length choice never inherits an old capture.
+NCU_DRAM_BYTES_PER_LAUNCH = {
+    ("ct256_y90_lu177_i131", "kf_x_inv", (280, 288, 280)): 142_640_128 + 37_710_592,
+}
 
 
 def make_inputs(wl):
@@ -75,10 +79,11 @@ def make_inputs(wl):
 
 
 def byte_model(shape, kmax, nk, density):
-    """Algorithmic HBM bytes per pass launch of the pruned 5-pass R2C pipeline at the
-    minimal padding P = N + K - 1 (padding beyond that is the implementation's cost).
-    x_fwd: 4V + A; y_fwd: A + By; z: per kernel By + S + By (multi-kernel launch counts
-    every kernel); y_inv: By + A; x_inv: A + 4V (+4V density)."""
+    """Algorithmic HBM bytes per STEP of each pass of the pruned 5-pass R2C pipeline at the
+    minimal padding P = N + K - 1 (padding beyond that is the implementation's cost), the
+    forward part counted once and the z pass / inverse per kernel:
+    x_fwd 4V + A; y_fwd A + By; z By + nk (By + S); y_inv nk (By + A);
+    x_inv nk (A + 4V) + 4V density (the density rows are read once for all kernels)."""
     n0, n1, n2 = shape
     p = [n + k - 1 for n, k in zip(shape, kmax)]
     h = p[2] // 2 + 1
@@ -86,16 +91,17 @@ def byte_model(shape, kmax, nk, density):
     a = 8 * n0 * n1 * h
     by = 8 * p[1] * n0 * h
     s = 4 * p[0] * p[1] * h
-    return {
+    m = {
         "x_fwd": 4 * v + a,
         "y_fwd": a + by,
-        "z_fwd_mul_inv": nk * (2 * by + s),
-        "y_inv": by + a,
-        "x_inv": a + 4 * v + (4 * v if density else 0),
-        "_per_step": (4 * v + a) + (a + by) + nk * (2 * by + s) + nk * (by + a) + nk * (a + 4 * v + (4 * v if density else 0)),
-        "_compulsory_per_step": 4 * v * (1 + (1 if density else 0) + nk) + nk * s,
-        "_p_min": p,
+        "z_fwd_mul_inv": by + nk * (by + s),
+        "y_inv": nk * (by + a),
+        "x_inv": nk * (a + 4 * v) + (4 * v if density else 0),
     }
+    m["_per_step"] = sum(m.values())
+    m["_compulsory_per_step"] = 4 * v * (1 + (1 if density else 0) + nk) + nk * s
+    m["_p_min"] = p
+    return m
 
 
 def load_peaks():
@@ -165,10 +171,29 @@ class ClockSampler:
 
 def cpu_reference_conv(act, rho, kernel):
     """The reference operator (core/kernel_convolution.py:71-74) in float64 on zero-padded
-    inputs, cropped, density-divided: the CPU path a reference user runs."""
+    inputs, cropped, density-divided: the same linear convolution this package computes."""
     from oracle import conv as oc
     d = oc.linear_conv_same(act.astype(np.float64), kernel)
     return oc.density_scale(d, rho)
+
+
+def cpu_reference_stock(act, kernel):
+    """The reference operator exactly as core/kernel_convolution.py:71-74 runs it: float64,
+    unpadded (circular), np.fft.ifftn(np.fft.fftn(A) * np.fft.fftn(K, A.shape)).real."""
+    from oracle import conv as oc
+    return oc.reference_circular_conv(act.astype(np.float64), kernel)
+
+
+def oracle_errors(act, rho, wl, dose, refs=None):
+    """Max / mean error of each nuclide's dose map (numpy [nk, *shape]) against the FP64
+    oracle (checker only, outside every timed region); with a density map also the
+    error of the energy per voxel D * rho and of the dose in tissue (rho >= 0.2).
+    Returns (errors, refs)."""
+    from oracle import conv as oc
+    if refs is None:
+        refs = oc.linear_conv_same_multi(act, reference_kernels(wl), density=rho)
+    errs = {nuc: oc.error_stats(dose[i], refs[i], density=rho) for i, nuc in enumerate(wl["nuclides"])}
+    return errs, refs
 
 
 def reference_kernels(wl):
@@ -195,6 +220,11 @@ def _ref_conv(i):
     return i
 
 
+def _ref_stock(i):
+    cpu_reference_stock(_REF["act"], _REF["ks"][i % len(_REF["ks"])])
+    return i
+
+
 def reference_workers(shape) -> int:
     """Host cores to run reference convolutions on: all of them, bounded by the memory
     one float64 FFT convolution of this shape needs (about 10 padded complex volumes)."""
@@ -213,24 +243,34 @@ def run_reference(args, wl, rank):
     """Reference arm: the reference's CPU convolution operator on this host's cores.  numpy's
     FFT runs on one thread, so the cores are used the way a reference user would use them for
     many volumes: one full-size nuclide convolution per worker process, all at once; a step is
-    one convolution on every worker."""
+    one convolution on every worker.  The line's value is the operator exactly as the
+    reference runs it (unpadded, circular: core/kernel_convolution.py:71-74); ``padded_linear``
+    times the same operator on zero-padded inputs with the density divide, which is the
+    linear convolution this package computes (fewer steps: it is only reported)."""
     if rank != 0:
         return
     import multiprocessing as mp
     from concurrent.futures import ProcessPoolExecutor
     workers = reference_workers(wl["shape"])
     vox = int(np.prod(wl["shape"]))
+
+    def timed(ex, fn, steps, warmup):
+        for w in range(warmup):
+            list(ex.map(fn, range(w * workers, (w + 1) * workers)))
+        times = []
+        for i in range(steps):
+            t0 = time.perf_counter()
+            list(ex.map(fn, range(i * workers, (i + 1) * workers)))
+            times.append(time.perf_counter() - t0)
+        return float(np.sum(times))
+
     with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"),
                              initializer=_ref_init, initargs=(args.workload,)) as ex:
-        for w in range(args.warmup):
-            list(ex.map(_ref_conv, range(w * workers, (w + 1) * workers)))
-        times = []
-        for i in range(args.steps):
-            t0 = time.perf_counter()
-            list(ex.map(_ref_conv, range(i * workers, (i + 1) * workers)))
-            times.append(time.perf_counter() - t0)
-    t = float(np.sum(times))
+        t = timed(ex, _ref_stock, args.steps, args.warmup)
+        pad_steps = min(args.steps, 3)
+        t_pad = timed(ex, _ref_conv, pad_steps, 1)
     value = vox * workers * args.steps / t / 1e9
+    value_pad = vox * workers * pad_steps / t_pad / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
@@ -238,8 +278,12 @@ def run_reference(args, wl, rank):
         "config": config_dict(args.workload, wl),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
                          "sample": f"per step one full {wl['shape']} convolution on each of {workers} worker "
-                                   "processes (nuclides in turn), numpy float64 FFT of the reference operator on "
-                                   "zero-padded inputs + density divide"},
+                                   "processes (nuclides in turn): the reference operator exactly as "
+                                   "kernel_convolution.py:71-74 runs it, numpy float64, unpadded circular"},
+        "padded_linear": {"value": value_pad, "unit": UNIT, "steps": pad_steps, "cores": workers,
+                          "ms_per_step": 1e3 * t_pad / pad_steps,
+                          "sample": "the same operator on zero-padded inputs (P = N + K - 1), cropped, density "
+                                    "divide: the linear density-scaled convolution the GPU arm computes"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -282,7 +326,9 @@ def measure_mc(device, n_hist=10_000_000, reps=3):
     plan.close()
     t = float(np.median(ms))
     return {"value": n_hist / (t / 1e3) / 1e6, "unit": "Mhistories/s", "ms_per_run": t, "histories": n_hist,
-            "workload": "Lu-177 beta+gamma, 128^3 CT phantom at 3 mm, dose-rate map included"}
+            "workload": "Lu-177 beta+gamma, 128^3 CT phantom at 3 mm, dose-rate map included",
+            "parity": "unpinned against the reference (its Monte Carlo cannot run); energy grids bit-identical to "
+                      "this package's C restatement of the same transport"}
 
 
 def measure_fit(device, shape=(256, 256, 256), reps=2):
@@ -513,6 +559,8 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
         "mc_histories_per_batch": hb, "mc_ms_10_batches": mc_ms, "mc_median_rel_se": rse_med,
         "mc_to_1pct_ms": mc_1pct_ms, "nn_vs_mc_1pct_speedup": mc_1pct_ms / nn_ms,
         "whole_body_512x512x400": large,
+        "parity": "U-Net layers checked against a float64 restatement of this package's own network (the "
+                  "reference has none: unpinned against the reference); MC unpinned as in 'mc'",
     }
 
 
@@ -547,6 +595,7 @@ def measure_unet_large(device, net, reps=2):
         e1.synchronize()
         inf_ms.append(e0.elapsed_time(e1))
     net.status()
+    kshape = conv._kernel_specs(vox)[0][0].shape
     conv.close()
     c, i = float(np.median(conv_ms)), float(np.median(inf_ms))
     nvox = float(np.prod(shape))
@@ -554,6 +603,19 @@ def measure_unet_large(device, net, reps=2):
            "nn_corrected_gvox_s": nvox / ((c + i) / 1e3) / 1e9,
            "unet_inference_tflops": lc.conv_flops(shape) / (i / 1e3) / 1e12,
            "device_memory_peak_gb": torch.cuda.max_memory_allocated(device) / 1e9}
+    # plain convolution against the FP64 oracle on a slab of 16 z planes through the middle:
+    # the linear convolution of the input planes within the kernel's reach of the slab
+    # gives the exact dose of the slab's planes (checker, outside the timed region)
+    from oracle import conv as oc
+    from pyvoxeldosimetry_gb300.data import nuclides as nd
+    z0, nz, hz = shape[0] // 2 - 8, 16, kshape[0] // 2
+    act_s = a[z0 - hz:z0 + nz + hz].cpu().numpy()
+    rho_s = r[z0 - hz:z0 + nz + hz].cpu().numpy()
+    kk = nd.analytic_profile("Y90", vox, kshape)
+    ref = oc.linear_conv_same_multi(act_s, [kk / kk.sum() * nd.gy_per_bq_s_scale("Y90", vox)], density=rho_s)[0]
+    res["plain_conv_error_vs_fp64_oracle"] = dict(oc.error_stats(d[z0:z0 + nz].cpu().numpy(), ref[hz:hz + nz],
+                                                                 density=rho_s[hz:hz + nz]),
+                                                  slab=f"z {z0}..{z0 + nz - 1} of {shape[0]}")
     net._ws.clear()
     del a, r, d, out
     torch.cuda.empty_cache()
@@ -687,6 +749,7 @@ def main():
     ap.add_argument("--workload", default="ct256_y90_lu177_i131", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-check", action="store_true", help="skip the error check against the FP64 oracle")
     ap.add_argument("--no-extras", action="store_true", help="skip the MC, fit and batch sub-measurements")
     ap.add_argument("--batch-volumes", type=int, default=8,
                     help="volumes of the 64-volume seeded uneven batch to run in the batch sub-measurement")
@@ -778,12 +841,15 @@ def main():
     peak, peak_src = load_peaks()
     dom = max(PASS_NAMES, key=lambda k: pass_ms[k])
     avg_s = pass_ms[dom] / max(pass_n[dom], 1) / 1e3
-    achieved = bm[dom] / avg_s / 1e9
-    traffic = NCU_DRAM_BYTES_PER_LAUNCH.get(args.workload, {}).get(PASS_KERNELS[PASS_NAMES.index(dom)])
+    launch_bytes = bm[dom] * args.steps / max(pass_n[dom], 1)  # the pass's bytes per step over its launches
+    achieved = launch_bytes / avg_s / 1e9
+    traffic = NCU_DRAM_BYTES_PER_LAUNCH.get((args.workload, PASS_KERNELS[PASS_NAMES.index(dom)],
+                                             tuple(plan.fft_shape)))
     step_s = total_ms / args.steps / 1e3
     roofline = {"bound": "hbm", "kernel": PASS_KERNELS[PASS_NAMES.index(dom)], "achieved": achieved,
                 "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                "algorithmic_bytes_per_launch": bm[dom], "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": launch_bytes, "launches_per_step": pass_n[dom] / args.steps,
+                "peak_source": peak_src,
                 "pass_ms_per_step": {k: pass_ms[k] / args.steps for k in PASS_NAMES},
                 "pipeline_achieved": bm["_per_step"] / step_s / 1e9,
                 "pipeline_frac": bm["_per_step"] / step_s / 1e9 / peak,
@@ -795,6 +861,12 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded phantom)",
             "config": config_dict(args.workload, wl), "roofline": roofline, "gpu_launches": launches,
             "clocks": clk.summary()}
+
+    # errors of one step's output against the FP64 oracle (checker, outside the timed region)
+    refs = None
+    if rank == 0 and not args.no_check:
+        errs, refs = oracle_errors(act, rho, wl, out_d.cpu().numpy())
+        line["error_vs_fp64_oracle"] = errs
 
     # end to end through the public API from pinned host memory
     if not args.no_e2e:
@@ -820,6 +892,38 @@ def main():
                        "d2h_bytes_per_step": 4 * vox * nk, "ms_per_step": e2e_ms / args.steps,
                        "wall_ms_per_step": 1e3 * wall / args.steps,
                        "api": "KernelConvolutionCalculator.calculate_dose_rate(pinned CPU tensors)"}
+        if rank == 0 and not args.no_check:
+            line["e2e"]["error_vs_fp64_oracle"] = oracle_errors(act, rho, wl, out_h.numpy(), refs)[0]
+        # the drop-in user's call: pageable numpy in, new numpy arrays out, through the
+        # reference's facade (DoseCalculator.calculate_dose, single timepoint), host wall clock
+        from pyvoxeldosimetry_gb300.core.dose_calculator import DoseCalculator
+        dc = DoseCalculator(wl["nuclides"], method="kernel",
+                            config={"kernel_size": wl["ksize"], "device": device})
+        act_np = np.ascontiguousarray(act)
+        rho_np = np.ascontiguousarray(rho) if rho is not None else None
+        for i in range(args.warmup):
+            res = dc.calculate_dose(activity_maps=[act_np], time_points=[0.0], voxel_size=vs,
+                                    tissue_densities=rho_np)
+        barrier()
+        np_ms = []
+        for i in range(args.steps):
+            t0 = time.perf_counter()
+            res = dc.calculate_dose(activity_maps=[act_np], time_points=[0.0], voxel_size=vs,
+                                    tissue_densities=rho_np)
+            np_ms.append(1e3 * (time.perf_counter() - t0))
+        barrier()
+        np_total = max_over_ranks(float(np.sum(np_ms)), device)
+        d_np = res.dose_rate_maps[0]
+        line["e2e_numpy"] = {"value": job_throughput(world, nk * vox, args.steps, np_total), "unit": UNIT,
+                             "h2d_bytes_per_step": 4 * vox * (2 if rho is not None else 1),
+                             "d2h_bytes_per_step": 4 * vox * nk, "ms_per_step": np_total / args.steps,
+                             "api": "DoseCalculator(method='kernel').calculate_dose(activity_maps=[numpy], "
+                                    "tissue_densities=numpy) -> new numpy arrays (pageable host memory, host "
+                                    "wall clock per call)",
+                             "output": f"{type(d_np).__name__} {getattr(d_np, 'dtype', '')} {list(d_np.shape)}"}
+        if rank == 0 and not args.no_check:
+            line["e2e_numpy"]["error_vs_fp64_oracle"] = oracle_errors(act, rho, wl, d_np, refs)[0]
+        dc.calculator.close()
 
     if not args.no_extras and rank == 0:  # sub-measurements of one GPU; only rank 0 prints
         line["mc"] = measure_mc(device)
@@ -834,12 +938,29 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         ks = reference_kernels(wl)
         t0 = time.perf_counter()
-        cpu_reference_conv(act, rho, ks[0])
+        cpu_reference_stock(act, ks[0])
         dt = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        cpu_reference_conv(act, rho, ks[0])
+        dt_pad = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": vox / dt / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"one full {list(shape)} {wl['nuclides'][0]} convolution: numpy float64 "
-                                          "FFT of the reference operator on zero-padded inputs + density divide",
-                                "seconds": dt}
+                                "sample": f"one full {list(shape)} {wl['nuclides'][0]} convolution: the reference "
+                                          "operator exactly as kernel_convolution.py:71-74 runs it (numpy float64, "
+                                          "unpadded circular, one thread)",
+                                "seconds": dt,
+                                "padded_linear": {"value": vox / dt_pad / 1e9, "seconds": dt_pad,
+                                                  "sample": "the same operator on zero-padded inputs + density "
+                                                            "divide (the linear convolution computed here)"}}
+        line["vs_cpu_baseline_1core"] = {
+            "device_resident_vs_stock": value / line["cpu_baseline"]["value"],
+            "device_resident_vs_padded": value / line["cpu_baseline"]["padded_linear"]["value"]}
+        if "e2e" in line:
+            line["vs_cpu_baseline_1core"]["e2e_vs_stock"] = line["e2e"]["value"] / line["cpu_baseline"]["value"]
+            line["vs_cpu_baseline_1core"]["e2e_vs_padded"] = \
+                line["e2e"]["value"] / line["cpu_baseline"]["padded_linear"]["value"]
+        if "e2e_numpy" in line:
+            line["vs_cpu_baseline_1core"]["e2e_numpy_vs_stock"] = \
+                line["e2e_numpy"]["value"] / line["cpu_baseline"]["value"]
     if world > 1:
         dist.destroy_process_group()
     if rank == 0:

@@ -169,11 +169,15 @@ pvd_status pvd_plan_status(const pvd_plan* plan);
  * PVD_ERR_UNSUPPORTED and a message giving the bytes needed.
  *
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress, with that device current) and caches it; make that
- * first call before any stream capture.  Every call uses the same array: calls
- * that can overlap on the GPU (other streams, other host threads) race and
- * must be serialised by the caller.  The kernel upload is a plain host-to-device
- * copy on `stream`. */
+ * (cudaGetSymbolAddress, with that device current) and caches it for the life
+ * of the process; make that first call before any stream capture, and do not
+ * use this entry point across a cudaDeviceReset (or any destruction of the
+ * device's primary context), after which the cached address is stale.  Every
+ * call uses the same array: calls that can overlap on the GPU (other streams,
+ * other host threads) race and must be serialised by the caller.  The kernel
+ * upload is a plain host-to-device copy on `stream` from the caller's
+ * `kernel_h`.  With PVD_KERNEL_NORMALIZE a kernel whose sum is zero or not
+ * finite is rejected with PVD_ERR_NUMERIC, as pvd_plan_set_kernel does. */
 #define PVD_STATIC_SCRATCH_BYTES (64ull << 20)
 #define PVD_STATIC_MAX_DEVICES 64
 pvd_status pvd_conv_execute_static(const float* activity_d, const float* density_d, float* dose_d,

@@ -152,6 +152,10 @@ class BatchDoseCalculator:
         shape = tuple(it["cum"].shape)
         return it["params"].view(4, *shape), it["auc"].view(shape), it["ok"].view(shape).bool()
 
+    def cumulated(self, i: int) -> torch.Tensor:
+        """Cumulated activity (Bq s, float32) of volume i: the convolution's input."""
+        return self._items[i]["cum"]
+
     def __del__(self):
         try:
             self.close()

@@ -193,22 +193,23 @@ __global__ void __launch_bounds__(NT) k_x_fwd(ActIn in, float2* __restrict__ out
 
 // ---------------------------------------------------------------------------
 // passes 2 and 4: y-axis C2C over columns, zero-pad input rows >= nin, keep
-// output rows < nout.  blockIdx.x: column tile, blockIdx.y: z slab.
+// output rows < nout.  blockIdx.x: column tile, blockIdx.y: z slab, blockIdx.z:
+// kernel slot (the inverse pass runs in place in each slot's buffer).
 // ---------------------------------------------------------------------------
 template <bool INV>
-__global__ void __launch_bounds__(NT) k_y(const float2* __restrict__ in, float2* __restrict__ out, int nin, int nout,
-                                          int HS, FftLen f, const float2* __restrict__ twg) {
+__global__ void __launch_bounds__(NT) k_y(ColSet io, int nin, int nout, int HS, FftLen f,
+                                          const float2* __restrict__ twg) {
   extern __shared__ float2 sm[];
   float2* tw = sm;
   float2* a = sm + f.L;
   float2* b = a + f.L * TXP;
   load_twiddles(tw, twg, f.L);
   const int kx0 = blockIdx.x * TX;
-  const float2* src = in + (long long)blockIdx.y * nin * HS + kx0;
-  float2* dst = out + (long long)blockIdx.y * nout * HS + kx0;
+  const float2* src = pick(io.in, blockIdx.z) + (long long)blockIdx.y * io.in_slab + kx0;
+  float2* dst = pick(io.out, blockIdx.z) + (long long)blockIdx.y * io.out_slab + kx0;
   for (int idx = threadIdx.x; idx < TX * f.L; idx += NT) {
     const int n = idx / TX, c = idx % TX;
-    a[n * TXP + c] = (n < nin) ? src[(long long)n * HS + c] : make_float2(0.f, 0.f);
+    a[n * TXP + c] = (n < nin) ? __ldcg(src + (long long)n * HS + c) : make_float2(0.f, 0.f);
   }
   __syncthreads();
   float2* r = fft_tile<INV>(a, b, f, tw);
@@ -280,11 +281,13 @@ __global__ void __launch_bounds__(NT) k_z(const float2* __restrict__ in, OutSet 
 }
 
 // ---------------------------------------------------------------------------
-// pass 5: x-axis inverse C2R of pairs of rows, crop, scale, density.
+// pass 5: x-axis inverse C2R of pairs of rows, crop, scale, density, for the
+// kernel slots of `io` in turn (row r = z * N1 + y of slot s at
+// io.in[s] + (z * pitch + y) * HS).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NT) k_x_inv(const float2* __restrict__ in, float* __restrict__ out,
-                                              const float* __restrict__ rho, int nrows, int N2, int HS, float scale,
-                                              FftLen f, const float2* __restrict__ twg) {
+__global__ void __launch_bounds__(NT) k_x_inv(XInvSet io, const float* __restrict__ rho, int nrows, int N1,
+                                              int pitch, int N2, int HS, float scale, FftLen f,
+                                              const float2* __restrict__ twg) {
   extern __shared__ float2 sm[];
   float2* tw = sm;
   float2* a = sm + f.L;
@@ -292,41 +295,47 @@ __global__ void __launch_bounds__(NT) k_x_inv(const float2* __restrict__ in, flo
   load_twiddles(tw, twg, f.L);
   const long long row0 = (long long)blockIdx.x * (2 * TX);
   const int H = f.L / 2 + 1;
-  for (int idx = threadIdx.x; idx < TX * H; idx += NT) {
-    const int m = idx / H, k = idx - (idx / H) * H;
-    const long long ra = row0 + 2 * m, rb = ra + 1;
-    float2 xa = (ra < nrows) ? in[ra * HS + k] : make_float2(0.f, 0.f);
-    float2 xb = (rb < nrows) ? in[rb * HS + k] : make_float2(0.f, 0.f);
-    if (k == 0 || 2 * k == f.L) {  // DC / Nyquist bins of a real row are real
-      xa.y = 0.f;
-      xb.y = 0.f;
-    }
-    a[k * TXP + m] = make_float2(xa.x - xb.y, xa.y + xb.x);  // Xa + i Xb
-    const int kk = f.L - k;
-    if (k > 0 && kk >= H) a[kk * TXP + m] = make_float2(xa.x + xb.y, xb.x - xa.y);  // conj Xa + i conj Xb
-  }
-  __syncthreads();
-  float2* r = fft_tile<true>(a, b, f, tw);
-  for (int idx = threadIdx.x; idx < TX * N2; idx += NT) {
-    const int m = idx / N2, n = idx - (idx / N2) * N2;
-    const long long ra = row0 + 2 * m, rb = ra + 1;
-    const float2 z = r[n * TXP + m];
-    if (ra < nrows) {
-      float v = z.x * scale;
-      if (rho) {
-        const float d = __ldg(rho + ra * N2 + n);
-        v = (d > 0.f) ? v / d : 0.f;
+  for (int sl = 0; sl < io.n; ++sl) {
+    const float2* in = pick(io.in, sl);
+    float* out = pick(io.out, sl);
+    for (int idx = threadIdx.x; idx < TX * H; idx += NT) {
+      const int m = idx / H, k = idx - (idx / H) * H;
+      const long long ra = row0 + 2 * m, rb = ra + 1;
+      const long long za = ra / N1, zb = rb / N1;
+      float2 xa = (ra < nrows) ? in[(za * pitch + (ra - za * N1)) * HS + k] : make_float2(0.f, 0.f);
+      float2 xb = (rb < nrows) ? in[(zb * pitch + (rb - zb * N1)) * HS + k] : make_float2(0.f, 0.f);
+      if (k == 0 || 2 * k == f.L) {  // DC / Nyquist bins of a real row are real
+        xa.y = 0.f;
+        xb.y = 0.f;
       }
-      out[ra * N2 + n] = v;
+      a[k * TXP + m] = make_float2(xa.x - xb.y, xa.y + xb.x);  // Xa + i Xb
+      const int kk = f.L - k;
+      if (k > 0 && kk >= H) a[kk * TXP + m] = make_float2(xa.x + xb.y, xb.x - xa.y);  // conj Xa + i conj Xb
     }
-    if (rb < nrows) {
-      float v = z.y * scale;
-      if (rho) {
-        const float d = __ldg(rho + rb * N2 + n);
-        v = (d > 0.f) ? v / d : 0.f;
+    __syncthreads();
+    float2* r = fft_tile<true>(a, b, f, tw);
+    for (int idx = threadIdx.x; idx < TX * N2; idx += NT) {
+      const int m = idx / N2, n = idx - (idx / N2) * N2;
+      const long long ra = row0 + 2 * m, rb = ra + 1;
+      const float2 z = r[n * TXP + m];
+      if (ra < nrows) {
+        float v = z.x * scale;
+        if (rho) {
+          const float d = __ldg(rho + ra * N2 + n);
+          v = (d > 0.f) ? v / d : 0.f;
+        }
+        out[ra * N2 + n] = v;
       }
-      out[rb * N2 + n] = v;
+      if (rb < nrows) {
+        float v = z.y * scale;
+        if (rho) {
+          const float d = __ldg(rho + rb * N2 + n);
+          v = (d > 0.f) ? v / d : 0.f;
+        }
+        out[rb * N2 + n] = v;
+      }
     }
+    __syncthreads();  // the tiles are free for the next slot
   }
 }
 
@@ -907,13 +916,20 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
     }
     {
       PassTimer t(p, 1, st);
+      ColSet io;
+      std::memset(&io, 0, sizeof(io));
+      io.in[0] = b1;
+      io.out[0] = b2;
+      io.in_slab = (long long)N1 * p->HS;
+      io.out_slab = (long long)p->P[1] * p->HS;
       if (p->tma)
         fy->ty_fwd<<<std::min(p->grid_yf, ctiles_y * (z1 - z0)), fy->threads, p->smem_tyf, st>>>(
-            p->m_yf, p->buf2, N1, p->P[1], z0, z1 - z0, ctiles_y, p->HS, p->yf_chunks, p->yf_boxr, p->tw[1], p->d_err);
+            p->m_yf, p->buf2, N1, p->P[1], z0, z1 - z0, ctiles_y, p->HS, io.out_slab, p->yf_chunks, p->yf_boxr,
+            p->tw[1], p->d_err);
       else if (fy)
-        fy->y_fwd<<<dim3(ctiles_y, z1 - z0), fy->threads, fy->smem_col, st>>>(b1, b2, N1, p->P[1], p->HS, p->tw[1]);
+        fy->y_fwd<<<dim3(ctiles_y, z1 - z0), fy->threads, fy->smem_col, st>>>(io, N1, p->P[1], p->HS, p->tw[1]);
       else
-        k_y<false><<<dim3(ctiles_y, z1 - z0), NT, p->smem_y, st>>>(b1, b2, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
+        k_y<false><<<dim3(ctiles_y, z1 - z0), NT, p->smem_y, st>>>(io, N1, p->P[1], p->HS, p->f[1], p->tw[1]);
       PVD_LAUNCH_CHECK("y_fwd");
     }
   }
@@ -946,45 +962,65 @@ static pvd_status conv_run(pvd_plan* p, const ActIn& in, const float* rho, float
       k_z<<<dim3(ctiles_z, p->P[1]), NT, p->smem_z, st>>>(p->buf2, os, N0, p->P[1], p->HS, p->f[0], p->tw[0]);
     PVD_LAUNCH_CHECK("z");
   }
-  // with host buffers the inverse x pass runs in z chunks: the first slot's chunk c
-  // waits only for density chunk c, and each chunk's dose goes back as soon as it is written
-  const int dchunks = hio ? std::min(PVD_DOSE_CHUNKS, N0) : 1;
-  for (int s = 0; s < p->nk; ++s) {
-    {
-      PassTimer t(p, 3, st);
-      if (p->tma)
+  // y inverse of every slot in one launch (blockIdx.z = slot), in place: rows 0..N1-1
+  // of each z slab of the slot's z-pass buffer
+  const long long zslab = (long long)p->P[1] * p->HS;
+  {
+    PassTimer t(p, 3, st);
+    if (p->tma) {
+      for (int s = 0; s < p->nk; ++s) {
         fy->ty_inv<<<std::min(p->grid_yi, ctiles_y * N0), fy->threads, p->smem_tyi, st>>>(
-            p->m_yi[s], p->buf1, p->P[1], N1, 0, N0, ctiles_y, p->HS, p->yi_chunks, p->yi_boxr, p->tw[1], p->d_err);
-      else if (fy)
-        fy->y_inv<<<dim3(ctiles_y, N0), fy->threads, fy->smem_col, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS,
-                                                                       p->tw[1]);
+            p->m_yi[s], p->buf3[s], p->P[1], N1, 0, N0, ctiles_y, p->HS, zslab, p->yi_chunks, p->yi_boxr, p->tw[1],
+            p->d_err);
+        PVD_LAUNCH_CHECK("y_inv");
+      }
+    } else {
+      ColSet io;
+      std::memset(&io, 0, sizeof(io));
+      for (int s = 0; s < p->nk; ++s) io.in[s] = io.out[s] = p->buf3[s];
+      io.in_slab = io.out_slab = zslab;
+      if (fy)
+        fy->y_inv<<<dim3(ctiles_y, N0, p->nk), fy->threads, fy->smem_col, st>>>(io, p->P[1], N1, p->HS, p->tw[1]);
       else
-        k_y<true><<<dim3(ctiles_y, N0), NT, p->smem_y, st>>>(p->buf3[s], p->buf1, p->P[1], N1, p->HS, p->f[1],
-                                                           p->tw[1]);
+        k_y<true><<<dim3(ctiles_y, N0, p->nk), NT, p->smem_y, st>>>(io, p->P[1], N1, p->HS, p->f[1], p->tw[1]);
       PVD_LAUNCH_CHECK("y_inv");
     }
-    PassTimer t(p, 4, st);
-    for (int c = 0; c < dchunks; ++c) {
-      const long long z0 = (long long)N0 * c / dchunks, z1 = (long long)N0 * (c + 1) / dchunks;
-      const long long r0 = z0 * N1, nr = (z1 - z0) * N1;  // rows of this chunk
-      if (nr == 0) continue;
-      if (hio && s == 0 && hio->rho) PVD_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_rho[c], 0));
-      const float2* in_c = p->buf1 + r0 * p->HS;
-      float* out_c = dose + s * vox + r0 * N2;
-      const float* rho_c = rho ? rho + r0 * N2 : nullptr;
-      const int xb = (int)((nr + rows_x - 1) / rows_x);
-      if (fx)
-        fx->x_inv<<<xb, fx->threads, fx->smem_row, st>>>(in_c, out_c, rho_c, (int)nr, N2, p->HS, out_scale, p->tw[2]);
-      else
-        k_x_inv<<<xb, NT, p->smem_x, st>>>(in_c, out_c, rho_c, (int)nr, N2, p->HS, out_scale, p->f[2], p->tw[2]);
-      PVD_LAUNCH_CHECK("x_inv");
-      if (hio) {  // this chunk goes back while the next one computes
-        cudaEvent_t ev = p->ev_dose[s * PVD_DOSE_CHUNKS + c];
-        PVD_CUDA_TRY(cudaEventRecord(ev, st));
-        PVD_CUDA_TRY(cudaStreamWaitEvent(p->s_d2h, ev, 0));
-        PVD_CUDA_TRY(cudaMemcpyAsync(hio->dose + s * vox + r0 * N2, out_c, sizeof(float) * nr * N2,
-                                     cudaMemcpyDeviceToHost, p->s_d2h));
+  }
+  // x inverse of every slot (up to XINV_SLOTS per launch): the density rows are read
+  // from HBM once per row block.  With host buffers it runs in z chunks: chunk c
+  // waits only for density chunk c, and each chunk's dose goes back as soon as it is
+  // written.
+  const int dchunks = hio ? std::min(PVD_DOSE_CHUNKS, N0) : 1;
+  PassTimer t(p, 4, st);
+  for (int c = 0; c < dchunks; ++c) {
+    const long long z0 = (long long)N0 * c / dchunks, z1 = (long long)N0 * (c + 1) / dchunks;
+    const long long r0 = z0 * N1, nr = (z1 - z0) * N1;  // rows of this chunk
+    if (nr == 0) continue;
+    if (hio && hio->rho) PVD_CUDA_TRY(cudaStreamWaitEvent(st, p->ev_rho[c], 0));
+    const float* rho_c = rho ? rho + r0 * N2 : nullptr;
+    const int xb = (int)((nr + rows_x - 1) / rows_x);
+    for (int g0 = 0; g0 < p->nk; g0 += XINV_SLOTS) {
+      XInvSet xs;
+      std::memset(&xs, 0, sizeof(xs));
+      xs.n = std::min(XINV_SLOTS, p->nk - g0);
+      for (int i = 0; i < xs.n; ++i) {
+        xs.in[i] = p->buf3[g0 + i] + z0 * zslab;
+        xs.out[i] = dose + (g0 + i) * vox + r0 * N2;
       }
+      if (fx)
+        fx->x_inv<<<xb, fx->threads, fx->smem_row, st>>>(xs, rho_c, (int)nr, N1, p->P[1], N2, p->HS, out_scale,
+                                                         p->tw[2]);
+      else
+        k_x_inv<<<xb, NT, p->smem_x, st>>>(xs, rho_c, (int)nr, N1, p->P[1], N2, p->HS, out_scale, p->f[2], p->tw[2]);
+      PVD_LAUNCH_CHECK("x_inv");
+    }
+    if (hio) {  // this chunk goes back while the next one computes
+      cudaEvent_t ev = p->ev_dose[c];
+      PVD_CUDA_TRY(cudaEventRecord(ev, st));
+      PVD_CUDA_TRY(cudaStreamWaitEvent(p->s_d2h, ev, 0));
+      for (int s = 0; s < p->nk; ++s)
+        PVD_CUDA_TRY(cudaMemcpyAsync(hio->dose + s * vox + r0 * N2, dose + s * vox + r0 * N2, sizeof(float) * nr * N2,
+                                     cudaMemcpyDeviceToHost, p->s_d2h));
     }
   }
   if (hio) {  // the caller's stream completes only after the last copy back
@@ -1131,9 +1167,9 @@ extern "C" pvd_status pvd_plan_destroy(pvd_plan* p) {
 // Allocation-free convolution (no counterpart in the reference).
 //
 // Some callers cannot allocate device memory: code that runs under a memory
-// budget enforced by a host framework that owns the allocator, plugins that
+// budget enforced by a host framework that owns the allocator, or plugins that
 // must not call cudaMalloc/cudaFree (they synchronise the device and would
-// stall the host application's streams), or callers inside stream capture.
+// stall the host application's streams).
 // pvd_conv_execute_static runs the same five-pass pipeline as a plan, with all
 // of its scratch (twiddles, kernel staging, spectrum, the two spectral work
 // buffers) carved out of one file-scope device array of PVD_STATIC_SCRATCH_BYTES.
@@ -1192,8 +1228,15 @@ extern "C" pvd_status pvd_conv_execute_static(const float* activity_d, const flo
   if (!std::isfinite(scale) || !std::isfinite(out_scale))
     return set_error(PVD_ERR_NUMERIC, "pvd_conv_execute_static: non-finite scale");
   const long long nk = (long long)k0 * k1 * k2;
-  for (long long i = 0; i < nk; ++i)
+  double host_sum = 0.0;
+  for (long long i = 0; i < nk; ++i) {
     if (!std::isfinite(kernel_h[i])) return set_error(PVD_ERR_NUMERIC, "pvd_conv_execute_static: non-finite kernel value");
+    host_sum += kernel_h[i];
+  }
+  // the same rule as pvd_plan_set_kernel: a kernel that sums to zero (or overflows) cannot
+  // be normalised; the device still computes the normalisation sum itself in FP64
+  if ((flags & PVD_KERNEL_NORMALIZE) && !(std::isfinite(host_sum) && host_sum != 0.0))
+    return set_error(PVD_ERR_NUMERIC, "pvd_conv_execute_static: kernel sum is zero or non-finite; cannot normalise");
 
   // plan on the stack: same length choice and pass kernels as pvd_plan_create (LINEAR, one slot)
   pvd_plan p;

@@ -23,12 +23,12 @@ constexpr int FZ_SLOTS = 4;    // kernel slots per z-pass launch
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
 
 typedef void (*KxFwdFn)(ActIn, float2*, int, int, int, const float2*);
-typedef void (*KxInvFn)(const float2*, float*, const float*, int, int, int, float, const float2*);
-typedef void (*KyFn)(const float2*, float2*, int, int, int, const float2*);
+typedef void (*KxInvFn)(XInvSet, const float*, int, int, int, int, int, float, const float2*);
+typedef void (*KyFn)(ColSet, int, int, int, const float2*);
 typedef void (*KzFn)(const float2*, OutSet, int, int, int, const float2*);
 // TMA-staged persistent column passes
-typedef void (*KtyFn)(const __grid_constant__ CUtensorMap, float2*, int, int, int, int, int, int, int, int,
-                      const float2*, int*);
+typedef void (*KtyFn)(const __grid_constant__ CUtensorMap, float2*, int, int, int, int, int, int, long long, int,
+                      int, const float2*, int*);
 typedef void (*KtzFn)(const __grid_constant__ CUtensorMap, OutSet, int, int, int, int, int, int, const float2*, int*);
 
 constexpr unsigned long long TMA_WAIT_NS = 2000000000ull;  // a tile that has not landed after 2 s is an error
@@ -53,25 +53,27 @@ __device__ __forceinline__ void load_tw(float2* tw, const float2* __restrict__ t
 }
 
 // ---------------------------------------------------------------------------
-// column pass (y axis): blockIdx.x = column tile, blockIdx.y = z slab
+// column pass (y axis): blockIdx.x = column tile, blockIdx.y = z slab,
+// blockIdx.z = kernel slot.  Loads bypass L1 (ld.global.cg): the inverse pass
+// writes its output over its own input.
 // ---------------------------------------------------------------------------
 template <int A, int B, bool INV>
-__global__ void __launch_bounds__(FTX* cmax(A, B)) kf_y(const float2* __restrict__ in, float2* __restrict__ out,
-                                                         int nin, int nout, int HS, const float2* __restrict__ twg) {
+__global__ void __launch_bounds__(FTX* cmax(A, B)) kf_y(ColSet io, int nin, int nout, int HS,
+                                                         const float2* __restrict__ twg) {
   constexpr int L = A * B, NTH = FTX * cmax(A, B);
   extern __shared__ float2 sm[];
   float2* tw = sm;
   float2* ex = sm + tw_slots(L);
   const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
   const int kx0 = blockIdx.x * FTX;
-  const float2* src = in + (long long)blockIdx.y * nin * HS + kx0 + c;
-  float2* dst = out + (long long)blockIdx.y * nout * HS + kx0 + c;
+  const float2* src = pick(io.in, blockIdx.z) + (long long)blockIdx.y * io.in_slab + kx0 + c;
+  float2* dst = pick(io.out, blockIdx.z) + (long long)blockIdx.y * io.out_slab + kx0 + c;
   float2 v[B];
   if (j < A) {
     static_for<B>([&](auto ib) {
       constexpr int b = decltype(ib)::value;
       const int n = j + A * b;
-      v[b] = (n < nin) ? src[(long long)n * HS] : make_float2(0.f, 0.f);
+      v[b] = (n < nin) ? __ldcg(src + (long long)n * HS) : make_float2(0.f, 0.f);
     });
   }
   load_tw<L>(tw, twg, NTH);
@@ -204,8 +206,9 @@ __device__ __forceinline__ void tma_issue_rows(float2* dst, const CUtensorMap* m
 template <int A, int B, bool INV>
 __global__ void __launch_bounds__(FTX* cmax(A, B)) kt_y(const __grid_constant__ CUtensorMap tin,
                                                          float2* __restrict__ out, int nin, int nout, int slab0,
-                                                         int nslab, int ctiles, int HS, int chunks, int boxr,
-                                                         const float2* __restrict__ twg, int* __restrict__ err) {
+                                                         int nslab, int ctiles, int HS, long long out_slab,
+                                                         int chunks, int boxr, const float2* __restrict__ twg,
+                                                         int* __restrict__ err) {
   constexpr int L = A * B, NTH = FTX * cmax(A, B);
   extern __shared__ __align__(128) float2 sm[];
   const int SR = max(chunks * boxr, L);
@@ -245,7 +248,7 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kt_y(const __grid_constant__ 
     }
     float2 w[A];
     four_step<A, B, INV, FTX, true>(v, w, stage, tw, c, j);
-    float2* dst = out + (long long)(slab0 + t / ctiles) * nout * HS + (t % ctiles) * FTX + c;
+    float2* dst = out + (long long)(slab0 + t / ctiles) * out_slab + (t % ctiles) * FTX + c;
     if (j < B) {
       static_for<A>([&](auto iq) {
         constexpr int q = decltype(iq)::value;
@@ -480,10 +483,14 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_fwd(
   }
 }
 
-// x inverse: C2R of pairs of half-spectrum rows, crop, scale, density.
+// x inverse: C2R of pairs of half-spectrum rows, crop, scale, density, for up to
+// XINV_SLOTS kernel slots in turn (one launch per row block and slot group: the
+// twiddles are loaded once and the density rows come from HBM once, the later
+// slots finding them in cache).  Row r = z * N1 + y of slot s is read at
+// io.in[s] + (z * pitch + y) * HS.
 template <int A, int B>
-__global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_inv(const float2* __restrict__ in, float* __restrict__ out,
-                                                             const float* __restrict__ rho, int nrows, int N2, int HS,
+__global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_inv(XInvSet io, const float* __restrict__ rho,
+                                                             int nrows, int N1, int pitch, int N2, int HS,
                                                              float scale, const float2* __restrict__ twg) {
   constexpr int L = A * B, NTH = FTX * cmax(A, B), H = L / 2 + 1, ROWS = 2 * FTX;
   constexpr int NWF = NTH / 32;  // full warps (the last warp is partial when max(A, B) is odd)
@@ -499,78 +506,87 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_inv(
   const int nr = (int)min((long long)ROWS, (long long)nrows - row0);
   load_tw<L>(tw, twg, NTH);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // every row of the tile in flight at once: asynchronous copies straight into shared memory
-  if (warp < NWF) {
-    for (int rr = warp; rr < nr; rr += NWF) {
-      const float2* src = in + (row0 + rr) * HS;
-      float2* dsm = ((rr & 1) ? hb : ha) + (rr >> 1) * S2;
-      constexpr int KU = (H + 31) / 32;
-#pragma unroll
-      for (int u = 0; u < KU; ++u) {
-        const int k = 32 * u + lane;
-        if (k < H) cp_async8(dsm + k, src + k);
-      }
-    }
-  }
-  cp_async_wait_all();
-  __syncthreads();
   const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
-  float2 v[B];
-  if (j < A) {
-    const bool va = 2 * c < nr, vb = 2 * c + 1 < nr;
-    static_for<B>([&](auto ib) {
-      constexpr int b = decltype(ib)::value;
-      const int n = j + A * b;
-      const bool lo = n < H;
-      const int k = lo ? n : L - n;
-      float2 xa = va ? ha[c * S2 + k] : make_float2(0.f, 0.f);
-      float2 xb = vb ? hb[c * S2 + k] : make_float2(0.f, 0.f);
-      if (k == 0 || 2 * k == L) {  // DC / Nyquist bins of a real row are real
-        xa.y = 0.f;
-        xb.y = 0.f;
-      }
-      // Z[n] = Xa[n] + i Xb[n] for n < H, conj Xa[L-n] + i conj Xb[L-n] above
-      v[b] = lo ? make_float2(xa.x - xb.y, xa.y + xb.x) : make_float2(xa.x + xb.y, xb.x - xa.y);
-    });
-  }
-  float2 X[A];
-  four_step<A, B, true, FTX, true>(v, X, buf, tw, c, j);
-  __syncthreads();
-  if (j < B) {
-    static_for<A>([&](auto iq) {
-      constexpr int q = decltype(iq)::value;
-      const int n = j + B * q;
-      if (n < N2) {
-        oc[(2 * c) * S + n] = X[q].x * scale;
-        oc[(2 * c + 1) * S + n] = X[q].y * scale;
-      }
-    });
-  }
-  __syncthreads();
-  if (warp < NWF) {
-    for (int rr = warp; rr < nr; rr += NWF) {
-      float* dst = out + (row0 + rr) * N2;
-      const float* dr = rho ? rho + (row0 + rr) * N2 : nullptr;
-      constexpr int NU = (L + 31) / 32;  // N2 <= L
-      float d[NU];
-      if (dr) {
+  static_for<XINV_SLOTS>([&](auto is) {
+    constexpr int sl = decltype(is)::value;
+    if (sl < io.n) {
+      const float2* in = io.in[sl];
+      // every row of the tile in flight at once: asynchronous copies straight into shared memory
+      if (warp < NWF) {
+        for (int rr = warp; rr < nr; rr += NWF) {
+          const int r = (int)row0 + rr, z = r / N1;  // rows of a launch fit in 32 bits (n0 n1 <= 4096^2)
+          const float2* src = in + ((long long)z * pitch + (r - z * N1)) * HS;
+          float2* dsm = ((rr & 1) ? hb : ha) + (rr >> 1) * S2;
+          constexpr int KU = (H + 31) / 32;
 #pragma unroll
-        for (int u = 0; u < NU; ++u) {
-          const int n = 32 * u + lane;
-          d[u] = (n < N2) ? __ldg(dr + n) : 1.f;
+          for (int u = 0; u < KU; ++u) {
+            const int k = 32 * u + lane;
+            if (k < H) cp_async8(dsm + k, src + k);
+          }
         }
       }
+      cp_async_wait_all();
+      __syncthreads();
+      float2 v[B];
+      if (j < A) {
+        const bool va = 2 * c < nr, vb = 2 * c + 1 < nr;
+        static_for<B>([&](auto ib) {
+          constexpr int b = decltype(ib)::value;
+          const int n = j + A * b;
+          const bool lo = n < H;
+          const int k = lo ? n : L - n;
+          float2 xa = va ? ha[c * S2 + k] : make_float2(0.f, 0.f);
+          float2 xb = vb ? hb[c * S2 + k] : make_float2(0.f, 0.f);
+          if (k == 0 || 2 * k == L) {  // DC / Nyquist bins of a real row are real
+            xa.y = 0.f;
+            xb.y = 0.f;
+          }
+          // Z[n] = Xa[n] + i Xb[n] for n < H, conj Xa[L-n] + i conj Xb[L-n] above
+          v[b] = lo ? make_float2(xa.x - xb.y, xa.y + xb.x) : make_float2(xa.x + xb.y, xb.x - xa.y);
+        });
+      }
+      float2 X[A];
+      four_step<A, B, true, FTX, true>(v, X, buf, tw, c, j);
+      __syncthreads();
+      if (j < B) {
+        static_for<A>([&](auto iq) {
+          constexpr int q = decltype(iq)::value;
+          const int n = j + B * q;
+          if (n < N2) {
+            oc[(2 * c) * S + n] = X[q].x * scale;
+            oc[(2 * c + 1) * S + n] = X[q].y * scale;
+          }
+        });
+      }
+      __syncthreads();
+      if (warp < NWF) {
+        float* out = io.out[sl];
+        for (int rr = warp; rr < nr; rr += NWF) {
+          float* dst = out + (row0 + rr) * N2;
+          const float* dr = rho ? rho + (row0 + rr) * N2 : nullptr;
+          constexpr int NU = (L + 31) / 32;  // N2 <= L
+          float d[NU];
+          if (dr) {
 #pragma unroll
-      for (int u = 0; u < NU; ++u) {
-        const int n = 32 * u + lane;
-        if (n < N2) {
-          float val = oc[rr * S + n];
-          if (dr) val = (d[u] > 0.f) ? val * __frcp_rn(d[u]) : 0.f;
-          dst[n] = val;
+            for (int u = 0; u < NU; ++u) {
+              const int n = 32 * u + lane;
+              d[u] = (n < N2) ? __ldg(dr + n) : 1.f;
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < NU; ++u) {
+            const int n = 32 * u + lane;
+            if (n < N2) {
+              float val = oc[rr * S + n];
+              if (dr) val = (d[u] > 0.f) ? val * __frcp_rn(d[u]) : 0.f;
+              dst[n] = val;
+            }
+          }
         }
       }
+      __syncthreads();  // the output tile (aliasing the row tiles) is read out before the next slot's rows land
     }
-  }
+  });
 }
 
 template <int A, int B>

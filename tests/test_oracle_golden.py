@@ -144,3 +144,18 @@ def test_restated_linspace_edges_equal_numpy(dtype):
         for bins in (1, 3, 7, 1000, 20000):
             np.testing.assert_array_equal(od.numpy_linspace_edges(first, last, bins),
                                           np.linspace(first, last, bins + 1, endpoint=True, dtype=dtype))
+
+
+def test_multi_kernel_oracle_equals_single_kernel_oracle():
+    """The shared-forward-transform float64 oracle used at full size equals the
+    complex-FFT restatement of the reference operator on small cases."""
+    rng = np.random.default_rng(5)
+    a = rng.random((13, 11, 17))
+    rho = rng.uniform(0.0, 2.0, a.shape)
+    ks = [rng.random((5, 5, 5)), rng.random((3, 7, 9)), rng.random((1, 1, 1))]
+    outs = oc.linear_conv_same_multi(a, ks, density=rho, workers=2)
+    for k, d in zip(ks, outs):
+        ref = oc.density_scale(oc.linear_conv_same(a, k), rho)
+        np.testing.assert_allclose(d, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+    st = oc.error_stats(outs[0] * (1 + 1e-6), outs[0])
+    assert 0.9e-6 < st["max_normwise"] < 1.1e-6 and st["mean_normwise"] <= st["max_normwise"]

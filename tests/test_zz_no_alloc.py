@@ -100,3 +100,35 @@ def test_static_entry_point_rejects_sizes_beyond_its_array():
                                      21, 21, 21, 1.0, 0, C.c_float(1.0), None)
     assert st == 6  # PVD_ERR_UNSUPPORTED, before any device work
     assert "static maximum" in N.last_error()
+
+
+def test_static_entry_point_capacity_128cube_15kernel():
+    """The size the header names as fitting the static array (128^3 with a 15^3 kernel)
+    runs and agrees with the plan path."""
+    from pyvoxeldosimetry_gb300 import _native as N
+    lib = N.load()
+    rng = np.random.default_rng(23)
+    shape = (128, 128, 128)
+    act = torch.from_numpy((rng.random(shape) * 1e5).astype(np.float32)).cuda()
+    k = radial_kernel(15, 1.8, 2.0)
+    out = torch.empty(shape, dtype=torch.float32, device="cuda")
+    ref = plan_dose(lib, act, None, k, 1.0, N.PVD_KERNEL_NORMALIZE, 1.0)
+    d = static_dose(lib, act, None, out, k, 1.0, N.PVD_KERNEL_NORMALIZE, 1.0)
+    assert rel_err(d, ref) <= TOL
+
+
+def test_static_entry_point_rejects_a_kernel_it_cannot_normalise():
+    """A kernel summing to zero (a difference kernel) cannot be normalised: the call
+    returns PVD_ERR_NUMERIC like pvd_plan_set_kernel, instead of an Inf/NaN dose."""
+    from pyvoxeldosimetry_gb300 import _native as N
+    lib = N.load()
+    k = np.zeros((3, 3, 3))
+    k[0, 1, 1], k[2, 1, 1] = 1.0, -1.0
+    act = torch.ones((8, 8, 8), dtype=torch.float32, device="cuda")
+    out = torch.empty_like(act)
+    st = lib.pvd_conv_execute_static(act.data_ptr(), None, out.data_ptr(), 8, 8, 8, k.ctypes.data, 3, 3, 3, 1.0,
+                                     N.PVD_KERNEL_NORMALIZE, C.c_float(1.0), None)
+    assert st == 5  # PVD_ERR_NUMERIC
+    assert "cannot normalise" in N.last_error()
+    d = static_dose(lib, act, None, out, k, 1.0, 0, 1.0)  # used as given, it is a valid kernel
+    assert np.isfinite(d).all()
