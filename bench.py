@@ -750,6 +750,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the error check against the FP64 oracle")
+    ap.add_argument("--pads", help="explicit FFT lengths P0,P1,P2 (default: the autotuner's choice)")
     ap.add_argument("--no-extras", action="store_true", help="skip the MC, fit and batch sub-measurements")
     ap.add_argument("--batch-volumes", type=int, default=8,
                     help="volumes of the 64-volume seeded uneven batch to run in the batch sub-measurement")
@@ -788,7 +789,11 @@ def main():
     vox = int(np.prod(shape))
     nk = len(wl["nuclides"])
     vs = (wl["voxel_mm"],) * 3
-    calc = KernelConvolutionCalculator(wl["nuclides"], config={"kernel_size": wl["ksize"], "device": device})
+    cfg = {"kernel_size": wl["ksize"], "device": device}
+    if args.pads:  # explicit FFT lengths instead of the autotuner's
+        cfg["autotune"] = False
+        cfg["pads"] = tuple(int(x) for x in args.pads.split(","))
+    calc = KernelConvolutionCalculator(wl["nuclides"], config=cfg)
     plan = calc._plan_for(shape, vs, device)
     act_d = torch.from_numpy(act).to(device)
     rho_d = torch.from_numpy(rho).to(device) if rho is not None else None

@@ -67,7 +67,12 @@ typedef enum {
  *                      ifftn(fftn(A) * fftn(K, A.shape)).real: circular,
  *                      unpadded, kernel placed at the array corner and
  *                      truncated to the volume shape where it is larger
- *                      (output shifted by k//2 relative to LINEAR). */
+ *                      (output shifted by k//2 relative to LINEAR).  Any
+ *                      volume shape: an axis whose length n is 7-smooth is
+ *                      transformed at length n; any other axis at a zero-
+ *                      padded length P >= 2n with a second copy of the kernel
+ *                      at offset P - n, which yields the same period-n
+ *                      convolution (pad[i] may give n or a length >= 2n). */
 enum { PVD_MODE_LINEAR = 0, PVD_MODE_CIRCULAR = 1 };
 
 /* pvd_conv_desc flags */
@@ -150,7 +155,8 @@ pvd_status pvd_plan_destroy(pvd_plan* plan);
 
 /* Device-side status of the plan's passes: PVD_ERR_TIMEOUT if a TMA tile load
  * of a column pass did not complete within its bounded wait (the pass then
- * left its tiles unwritten); PVD_OK otherwise.  Synchronises with the device. */
+ * left its tiles unwritten); PVD_OK otherwise.  A failure is reported once: the
+ * status word is cleared when it is read.  Synchronises with the device. */
 pvd_status pvd_plan_status(const pvd_plan* plan);
 
 /* Allocation-free convolution.  No counterpart in the reference.
@@ -444,6 +450,32 @@ pvd_status pvd_resample_separable(const float* src_d, int n0, int n1, int n2, fl
                                   float* scratch_d, long long scratch_elems, pvd_stream stream);
 
 /* ------------------------------------------------------------------------ */
+/* CT Hounsfield units -> tissue masks and density                            */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces TissueComposition.calculate_composition (tissue/composition.py:48-70)
+ * with its artefact handling (:72-93): with PVD_HU_ARTIFACTS, voxels above 2000 HU
+ * (metal) take the value of the Gaussian-smoothed image (sigma 1 voxel, as
+ * scipy.ndimage.gaussian_filter with its default radius 4 and 'reflect' boundary)
+ * of the image whose metal voxels and NaNs are 0, computed in FP64.  Then
+ *   masks_d (device uint8 [5][n] or NULL): 1 where the (corrected) HU lies in the
+ *     closed range of air [-1000, -900], lung [-900, -500], soft tissue [-100, 100],
+ *     bone [300, 3000], water [-10, 10], in that plane order (ranges overlap and
+ *     leave gaps exactly as the reference's do; NaN is in none);
+ *   density_d (device float32 [n] or NULL): mass density (g/cc) by linear
+ *     interpolation through the n_anchor (1..16, HU increasing) calibration points
+ *     (anchor_hu[i], anchor_rho[i]) (host arrays), clamped to the end values, 0 for
+ *     NaN.  The reference has no HU-to-density step; this map feeds the
+ *     density-scaled convolution (pvd_conv_execute's density_d);
+ *   hu_d (device float32 [n] or NULL): the corrected HU.
+ * ct_d: device float32 [n0][n1][n2].  Device buffers 16-byte aligned.  Enqueued on
+ * `stream`. */
+enum { PVD_HU_ARTIFACTS = 1 };
+pvd_status pvd_hu_composition(const float* ct_d, int n0, int n1, int n2, int flags, const float* anchor_hu,
+                              const float* anchor_rho, int n_anchor, unsigned char* masks_d, float* density_d,
+                              float* hu_d, pvd_stream stream);
+
+/* ------------------------------------------------------------------------ */
 /* Dose-point kernels                                                         */
 /* ------------------------------------------------------------------------ */
 
@@ -613,6 +645,25 @@ pvd_status pvd_unet_status(int* code, int reset);
 /* ------------------------------------------------------------------------ */
 /* Misc                                                                       */
 /* ------------------------------------------------------------------------ */
+
+/* Failure-path instrumentation (no counterpart in the reference, whose failure
+ * handling is a try/except around curve_fit, time_integration/curve_fitting.py:58-59).
+ *
+ * pvd_wait_check launches one small kernel that waits on an mbarrier phase that
+ * nothing will complete, through the same bounded wait and failure recording as
+ * the plan's TMA column passes (PVD_WAITCHECK_PLAN: the plan's status word, read
+ * and cleared by pvd_plan_status) or the U-Net's tensor-core pipeline
+ * (PVD_WAITCHECK_UNET: read by pvd_unet_status; plan ignored), with `limit_ns`
+ * (at most 2e9) in place of their 2 s bound.  No copy or MMA is issued, so
+ * nothing is in flight when the wait runs out; the kernel records
+ * PVD_ERR_TIMEOUT and returns, and the context stays usable.
+ *
+ * pvd_set_plan_alloc_cap caps the device bytes any one plan may hold (0 = no
+ * cap): a plan creation or kernel load that would exceed it fails with
+ * PVD_ERR_OOM exactly as a failed cudaMalloc does, freeing what it holds. */
+enum { PVD_WAITCHECK_PLAN = 0, PVD_WAITCHECK_UNET = 1 };
+pvd_status pvd_wait_check(int which, pvd_plan* plan, unsigned long long limit_ns, pvd_stream stream);
+pvd_status pvd_set_plan_alloc_cap(size_t bytes);
 
 /* Copy the calling thread's last error message into buf (NUL-terminated).
  * Returns the status of the last failing call on this thread (PVD_OK if none). */

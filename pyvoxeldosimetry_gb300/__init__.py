@@ -18,8 +18,11 @@ from .core.utils import calculate_dvh, load_dose_map, resample_dose_map, resampl
 from .data.dose_kernels import KernelFactory
 from .batch import BatchDoseCalculator
 from .core.learned_correction import NNCorrectedDoseCalculator, UNet3D
+from .tissue import TissueComposition
+from .data.mc_decay import load_decay_data
 
 __all__ = [
+    "TissueComposition", "load_decay_data",
     "NNCorrectedDoseCalculator",
     "UNet3D",
     "DosimetryCalculator",

@@ -44,14 +44,18 @@ EXPORTED_SYMBOLS = [
     "pvd_batch_execute", "pvd_batch_create", "pvd_batch_run", "pvd_batch_destroy",
     "pvd_roi_stats", "pvd_histogram", "pvd_dvh",
     "pvd_bspline_prefilter", "pvd_resample", "pvd_resample_separable",
+    "pvd_hu_composition",
     "pvd_radial_kernel",
     "pvd_unet_geometry", "pvd_unet_conv3d", "pvd_unet_wgrad_workspace", "pvd_unet_conv3d_wgrad",
     "pvd_unet_pack_weights", "pvd_unet_pack_input", "pvd_unet_pool", "pvd_unet_pool_backward",
     "pvd_unet_upsample", "pvd_unet_upsample_backward", "pvd_unet_head", "pvd_unet_head_loss_workspace",
     "pvd_unet_head_loss", "pvd_unet_apply_correction", "pvd_unet_input_maxima", "pvd_unet_bias_grad_workspace", "pvd_unet_bias_grad", "pvd_adam_step",
     "pvd_unet_status",
+    "pvd_wait_check", "pvd_set_plan_alloc_cap",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
 ]
+PVD_WAITCHECK_PLAN, PVD_WAITCHECK_UNET = 0, 1
+PVD_HU_ARTIFACTS = 1
 
 
 class PvdError(RuntimeError):
@@ -167,6 +171,7 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_histogram": (st, [vp, i, vp, i, C.c_longlong, vp, i, vp, vp]),
         "pvd_dvh": (st, [vp, i, vp, i, C.c_longlong, i, vp, vp, vp]),
         "pvd_bspline_prefilter": (st, [vp, vp, vp, i, i, i, vp]),
+        "pvd_hu_composition": (st, [vp, i, i, i, i, C.POINTER(f), C.POINTER(f), i, vp, vp, vp, vp]),
         "pvd_radial_kernel": (st, [C.POINTER(RadialTerm), i, d, i, i, i, C.POINTER(C.c_double), vp, vp]),
         "pvd_resample": (st, [vp, i, i, i, vp, i, i, i, C.POINTER(C.c_double), C.POINTER(C.c_double), i, f, vp]),
         "pvd_resample_separable": (st, [vp, i, i, i, vp, i, i, i, C.POINTER(C.c_double), C.POINTER(C.c_double), i, f,
@@ -193,6 +198,8 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_unet_bias_grad": (st, [C.POINTER(UnetGeom), vp, i, vp, vp, C.c_size_t, vp]),
         "pvd_adam_step": (st, [vp, vp, vp, vp, C.c_int64, f, f, f, f, f, i, vp]),
         "pvd_unet_status": (st, [C.POINTER(i), i]),
+        "pvd_wait_check": (st, [i, vp, C.c_ulonglong, vp]),
+        "pvd_set_plan_alloc_cap": (st, [C.c_size_t]),
         "pvd_last_error": (st, [C.c_char_p, C.c_size_t]),
         "pvd_version": (i, []),
         "pvd_launch_count": (C.c_uint64, [i]),

@@ -18,6 +18,8 @@ ValueErrors.  Changes:
   * timepoint maps are used as given: image registration (SimpleITK in the
     reference, core/image_registration.py) is outside this package, so maps must
     already be aligned;
+  * ``ct_image`` (Hounsfield units) may replace ``tissue_densities``: the density
+    comes from the GPU HU calibration of ``tissue.TissueComposition``;
   * ``config['single_timepoint_dose'] = 'physical_decay'`` also returns the
     absorbed dose of one timepoint under physical decay to infinity,
     D = dose_rate * T1/2 * 3600 / ln 2.
@@ -86,12 +88,19 @@ class DoseCalculator:
     def calculate_dose(self, activity_maps=None, time_points: Optional[List[float]] = None,
                        voxel_size: Tuple[float, float, float] = (1.0, 1.0, 1.0), tissue_densities=None,
                        accumulated_activity=None, integration_mode: str = "activity",
-                       integration_limit: Optional[float] = None) -> DoseCalculationResult:
+                       integration_limit: Optional[float] = None, ct_image=None) -> DoseCalculationResult:
         """Absorbed dose or dose rate depending on the input (routing of
-        core/dose_calculator.py:85-164)."""
+        core/dose_calculator.py:85-164).  ``ct_image`` (HU, same shape as the activity),
+        used when ``tissue_densities`` is not given, supplies the density through
+        TissueComposition's HU calibration (``config['hu_density_calibration']``,
+        metal-artefact step unless ``config['handle_artifacts']`` is False)."""
         if len(voxel_size) != 3:
             raise ValueError("voxel_size must be a tuple of length 3.")
         calc = self.calculator
+        if tissue_densities is None and ct_image is not None:
+            from ..tissue import TissueComposition
+            tissue_densities = TissueComposition(self.config).calculate_density(
+                ct_image, handle_artifacts=self.config.get("handle_artifacts", True))
 
         if accumulated_activity is not None:
             sec = SECONDS_PER[self.activity_sampler.units]

@@ -31,7 +31,8 @@ Differences from the reference, each deliberate:
     numpy out, CUDA tensor in -> CUDA tensor out);
   * the FFT lengths of a new (shape, kernel size) are chosen by timing the
     candidates once (``pyvoxeldosimetry_gb300.autotune``, cached on disk);
-    ``config['autotune'] = False`` takes the smallest fast length instead.
+    ``config['autotune'] = False`` takes the smallest fast length instead, and
+    ``config['pads'] = (P0, P1, P2)`` gives the lengths explicitly.
 """
 from __future__ import annotations
 
@@ -123,8 +124,8 @@ class KernelConvolutionCalculator(DosimetryCalculator):
             self._plan.close()
             self._plan = None
         kmax = tuple(max(k.shape[i] for k, _, _ in specs) for i in range(3))
-        pads = None
-        if self.mode == "linear" and self.config.get("autotune", True):
+        pads = self.config.get("pads")
+        if pads is None and self.mode == "linear" and self.config.get("autotune", True):
             from ..autotune import tune
             pads = tune(shape, kmax, len(specs), device=device)
         plan = ConvPlan(shape, kmax=kmax, n_kernels=len(specs), mode=self.mode, pad=pads, device=device)

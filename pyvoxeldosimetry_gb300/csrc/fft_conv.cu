@@ -26,6 +26,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -364,18 +365,29 @@ __global__ void k_scale_to_f32(const double* __restrict__ k, long long n, const 
     kf[i] = (float)(k[i] * fac);
 }
 
-// T1[m0][m1][kx] = sum_m2 k[m0][m1][m2] w2^(kx * ((m2 - o2) mod P2))
+// Placement of kernel index m along one axis of length P: at (m - o) mod P, and, when
+// img > 0, a second copy at (m + img) mod P.  The copy makes a convolution of period
+// P >= 2N into the circular convolution of period N (img = P - N): for an input that
+// is zero beyond N, output index i < N then receives A[(i - m) mod N] * K[m] exactly.
+// Returns the summed twiddle of the placed copies for frequency k.
+__device__ __forceinline__ float2 placed_twiddle(const float2* __restrict__ tw, int k, int m, int o, int img, int P) {
+  const int p = ((m - o) % P + P) % P;
+  float2 w = tw[(int)(((long long)k * p) % P)];
+  if (img > 0) w = cadd(w, tw[(int)(((long long)k * ((m + img) % P)) % P)]);
+  return w;
+}
+
+// T1[m0][m1][kx] = sum_m2 k[m0][m1][m2] w2^(kx * place(m2))
 __global__ void k_spec_x(const float* __restrict__ kf, float2* __restrict__ t1, int K0, int K1, int K2, int K2e,
-                         int o2, int P2, int H, const float2* __restrict__ tw2) {
+                         int o2, int img2, int P2, int H, const float2* __restrict__ tw2) {
   const long long total = (long long)K0 * K1 * H;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
     const int kx = (int)(i % H);
     const long long row = i / H;
     float2 acc = make_float2(0.f, 0.f);
     for (int m = 0; m < K2e; ++m) {
-      const int p = ((m - o2) % P2 + P2) % P2;
       const float v = kf[row * K2 + m];
-      const float2 w = tw2[(int)(((long long)kx * p) % P2)];
+      const float2 w = placed_twiddle(tw2, kx, m, o2, img2, P2);
       acc.x += v * w.x;
       acc.y += v * w.y;
     }
@@ -383,9 +395,9 @@ __global__ void k_spec_x(const float* __restrict__ kf, float2* __restrict__ t1, 
   }
 }
 
-// T2[m0][ky][kx] = sum_m1 T1[m0][m1][kx] w1^(ky * ((m1 - o1) mod P1))
+// T2[m0][ky][kx] = sum_m1 T1[m0][m1][kx] w1^(ky * place(m1))
 __global__ void k_spec_y(const float2* __restrict__ t1, float2* __restrict__ t2, int K0, int K1, int K1e, int o1,
-                         int P1, int H, const float2* __restrict__ tw1) {
+                         int img1, int P1, int H, const float2* __restrict__ tw1) {
   const long long total = (long long)K0 * P1 * H;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
     const int kx = (int)(i % H);
@@ -393,18 +405,17 @@ __global__ void k_spec_y(const float2* __restrict__ t1, float2* __restrict__ t2,
     const int m0 = (int)(i / ((long long)H * P1));
     float2 acc = make_float2(0.f, 0.f);
     for (int m = 0; m < K1e; ++m) {
-      const int p = ((m - o1) % P1 + P1) % P1;
       const float2 v = t1[((long long)m0 * K1 + m) * H + kx];
-      acc = cadd(acc, cmul(v, tw1[(int)(((long long)ky * p) % P1)]));
+      acc = cadd(acc, cmul(v, placed_twiddle(tw1, ky, m, o1, img1, P1)));
     }
     t2[i] = acc;
   }
 }
 
-// S[kz][ky][kx] = sum_m0 T2[m0][ky][kx] w0^(kz * ((m0 - o0) mod P0)); kx in [H, HS) -> 0.
+// S[kz][ky][kx] = sum_m0 T2[m0][ky][kx] w0^(kz * place(m0)); kx in [H, HS) -> 0.
 // SPEC_REAL_EVEN stores the real part for kz <= P0/2, ky <= P1/2 only.
-__global__ void k_spec_z(const float2* __restrict__ t2, void* __restrict__ spec, int mode, int K0e, int o0, int P0,
-                         int P1, int H, int HS, const float2* __restrict__ tw0) {
+__global__ void k_spec_z(const float2* __restrict__ t2, void* __restrict__ spec, int mode, int K0e, int o0, int img0,
+                         int P0, int P1, int H, int HS, const float2* __restrict__ tw0) {
   const int nz = (mode == SPEC_REAL_EVEN) ? P0 / 2 + 1 : P0;
   const int ny = (mode == SPEC_REAL_EVEN) ? P1 / 2 + 1 : P1;
   const long long total = (long long)nz * ny * HS;
@@ -415,9 +426,8 @@ __global__ void k_spec_z(const float2* __restrict__ t2, void* __restrict__ spec,
     float2 acc = make_float2(0.f, 0.f);
     if (kx < H) {
       for (int m = 0; m < K0e; ++m) {
-        const int p = ((m - o0) % P0 + P0) % P0;
         const float2 v = t2[((long long)m * P1 + ky) * H + kx];
-        acc = cadd(acc, cmul(v, tw0[(int)(((long long)kz * p) % P0)]));
+        acc = cadd(acc, cmul(v, placed_twiddle(tw0, kz, m, o0, img0, P0)));
       }
     }
     if (mode == SPEC_REAL_EVEN)
@@ -440,6 +450,7 @@ struct pvd_plan {
   int N[3] = {0, 0, 0};
   int P[3] = {0, 0, 0};
   int kmax[3] = {0, 0, 0};
+  int img[3] = {0, 0, 0};  // CIRCULAR axes with P >= 2N: offset of the kernel's image copy (P - N)
   int H = 0, HS = 0, nk = 0;
   FftLen f[3];
   float2* tw[3] = {nullptr, nullptr, nullptr};
@@ -481,7 +492,15 @@ struct pvd_plan {
 
 namespace {
 
+// Cap on the device bytes one plan may hold (0 = none): instrumentation that lets a
+// test make plan creation fail the way an exhausted device does, without exhausting it.
+std::atomic<size_t> g_plan_alloc_cap{0};
+
 pvd_status plan_alloc(pvd_plan* p, size_t bytes, void** out) {
+  const size_t cap = g_plan_alloc_cap.load();
+  if (cap && p->ws_bytes + bytes > cap)
+    return set_error(PVD_ERR_OOM, "plan workspace: " + std::to_string(p->ws_bytes + bytes) +
+                                      " bytes exceed the allocation cap of " + std::to_string(cap) + " bytes");
   void* ptr = nullptr;
   cudaError_t e = cudaMalloc(&ptr, bytes);
   if (e != cudaSuccess) {
@@ -609,12 +628,6 @@ pvd_status setup_tma(pvd_plan* p, int smem_max) {
   p->grid_yi = persistent_grid((const void*)fy->ty_inv, fy->threads, p->smem_tyi, p->dev);
   p->grid_z = persistent_grid((const void*)fz->tz, fz->threads, p->smem_tz, p->dev);
   if (p->grid_yf <= 0 || p->grid_yi <= 0 || p->grid_z <= 0) return PVD_OK;
-  void* ptr = nullptr;
-  pvd_status st = plan_alloc(p, sizeof(int), &ptr);
-  if (st != PVD_OK) return st;
-  p->d_err = (int*)ptr;
-  cudaError_t e = cudaMemset(p->d_err, 0, sizeof(int));
-  if (e != cudaSuccess) return cuda_error(e, "cudaMemset(status word)");
   p->tma = 1;
   return PVD_OK;
 }
@@ -641,24 +654,39 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
   for (int i = 0; i < 3; ++i) {
     p->N[i] = d->n[i];
     p->kmax[i] = d->kmax[i];
-    int need = (d->mode == PVD_MODE_LINEAR) ? d->n[i] + d->kmax[i] - 1 : d->n[i];
+    const int n = d->n[i];
     int L = d->pad[i];
-    if (!L) {
-      if (d->mode == PVD_MODE_CIRCULAR) {
-        L = need;
-      } else {  // prefer a length with register four-step kernels when it pads by <= 25 %
+    if (d->mode == PVD_MODE_CIRCULAR) {
+      // period n directly when n is 7-smooth; otherwise a zero-padded length >= 2n with
+      // the kernel's image copy at P - n, which gives the same period-n convolution
+      if (!L) {
+        if (is_smooth7(n)) {
+          L = n;
+        } else {
+          const int lf = fast_len_at_least(2 * n), ls = next_smooth7(2 * n);
+          L = (lf && lf <= ls) ? lf : ls;
+        }
+      }
+      if (L != n && L < 2 * n) {
+        delete p;
+        return set_error(PVD_ERR_ARG, "pvd_plan_create: CIRCULAR pad must be n or at least 2n");
+      }
+      p->img[i] = (L == n) ? 0 : L - n;
+    } else {
+      const int need = n + d->kmax[i] - 1;
+      if (!L) {  // prefer a length with register four-step kernels when it pads by <= 25 %
         const int lf = fast_len_at_least(need), ls = next_smooth7(need);
         L = (lf && (lf == ls || 4 * lf <= 5 * need)) ? lf : ls;
       }
-    }
-    if (L < need || (d->mode == PVD_MODE_CIRCULAR && L != need)) {
-      delete p;
-      return set_error(PVD_ERR_ARG, "pvd_plan_create: explicit pad too small (LINEAR needs n+kmax-1, CIRCULAR needs n)");
+      if (L < need) {
+        delete p;
+        return set_error(PVD_ERR_ARG, "pvd_plan_create: explicit pad too small (LINEAR needs n+kmax-1)");
+      }
     }
     if (!factorize(L, &p->f[i])) {
       delete p;
       return set_error(PVD_ERR_UNSUPPORTED, "pvd_plan_create: FFT length " + std::to_string(L) +
-                                                " has a prime factor > 7 (CIRCULAR mode needs 7-smooth dims)");
+                                                " has a prime factor > 7 (explicit pads must be 7-smooth)");
     }
     p->P[i] = L;
     p->fl[i] = fast_len(L);
@@ -723,6 +751,14 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
     for (int s = 1; s < p->nk && e == cudaSuccess; ++s) e = cudaMemset(p->buf3[s], 0, b2);
     if (e != cudaSuccess) st = cuda_error(e, "cudaMemset(workspace)");
   }
+  if (st == PVD_OK) {  // device status word of the plan's passes (bounded waits record here)
+    st = plan_alloc(p, sizeof(int), &ptr);
+    if (st == PVD_OK) {
+      p->d_err = (int*)ptr;
+      cudaError_t e = cudaMemset(p->d_err, 0, sizeof(int));
+      if (e != cudaSuccess) st = cuda_error(e, "cudaMemset(status word)");
+    }
+  }
   if (st == PVD_OK && (d->flags & PVD_PLAN_TMA)) st = setup_tma(p, smem_max);
   if (st != PVD_OK) {
     plan_free(p);
@@ -770,7 +806,8 @@ extern "C" pvd_status pvd_plan_set_kernel(pvd_plan* p, int slot, const double* k
   bool sym = (p->mode == PVD_MODE_LINEAR);
   for (int i = 0; i < 3; ++i) {
     o[i] = (p->mode == PVD_MODE_LINEAR) ? K[i] / 2 : 0;
-    Ke[i] = std::min(K[i], p->P[i]);
+    // CIRCULAR: the reference's fftn(K, A.shape) keeps the first n entries per axis
+    Ke[i] = std::min(K[i], (p->mode == PVD_MODE_LINEAR) ? p->P[i] : p->N[i]);
     if (K[i] % 2 == 0) sym = false;
   }
   for (long long i = 0; sym && i < nk; ++i) {
@@ -852,11 +889,11 @@ extern "C" pvd_status pvd_plan_set_kernel(pvd_plan* p, int slot, const double* k
   const int gs = 152 * 8;
   k_scale_to_f32<<<gs, NT>>>(kd, nk, norm ? sumd : nullptr, scale * inv_p, kf);
   count_launch();
-  k_spec_x<<<gs, NT>>>(kf, t1, k0, k1, k2, Ke[2], o[2], p->P[2], p->H, p->tw[2]);
+  k_spec_x<<<gs, NT>>>(kf, t1, k0, k1, k2, Ke[2], o[2], p->img[2], p->P[2], p->H, p->tw[2]);
   count_launch();
-  k_spec_y<<<gs, NT>>>(t1, t2, k0, k1, Ke[1], o[1], p->P[1], p->H, p->tw[1]);
+  k_spec_y<<<gs, NT>>>(t1, t2, k0, k1, Ke[1], o[1], p->img[1], p->P[1], p->H, p->tw[1]);
   count_launch();
-  k_spec_z<<<gs, NT>>>(t2, p->spec[slot], smode, Ke[0], o[0], p->P[0], p->P[1], p->H, p->HS, p->tw[0]);
+  k_spec_z<<<gs, NT>>>(t2, p->spec[slot], smode, Ke[0], o[0], p->img[0], p->P[0], p->P[1], p->H, p->HS, p->tw[0]);
   count_launch();
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -1152,7 +1189,38 @@ extern "C" pvd_status pvd_plan_status(const pvd_plan* p) {
   if (!p->d_err) return PVD_OK;
   int v = 0;
   PVD_CUDA_TRY(cudaMemcpy(&v, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
-  if (v) return set_error((pvd_status)v, "pvd_plan_status: a TMA tile load did not complete in time");
+  if (v) {  // reported once: the word is cleared for the plan's later work
+    PVD_CUDA_TRY(cudaMemset(p->d_err, 0, sizeof(int)));
+    return set_error((pvd_status)v, "pvd_plan_status: a bounded wait of a pass ran out (TMA tile load not complete)");
+  }
+  return PVD_OK;
+}
+
+namespace {
+// One CTA waits, through the TMA passes' own bounded wait, on a barrier phase that
+// nothing completes: no copy is issued, so nothing is in flight when the wait ends.
+__global__ void k_plan_wait_check(uint64_t limit_ns, int* err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (!cta_stage_wait(&bar, 0, limit_ns, err)) return;
+}
+}  // namespace
+
+namespace pvd {
+pvd_status plan_wait_check(pvd_plan* p, unsigned long long limit_ns, cudaStream_t st) {
+  if (!p) return set_error(PVD_ERR_ARG, "pvd_wait_check: null plan");
+  k_plan_wait_check<<<1, 128, 0, st>>>(limit_ns, p->d_err);
+  PVD_LAUNCH_CHECK("k_plan_wait_check");
+  return PVD_OK;
+}
+}  // namespace pvd
+
+extern "C" pvd_status pvd_set_plan_alloc_cap(size_t bytes) {
+  g_plan_alloc_cap.store(bytes);
   return PVD_OK;
 }
 
@@ -1354,11 +1422,11 @@ extern "C" pvd_status pvd_conv_execute_static(const float* activity_d, const flo
   float2* t2 = p.buf1;
   k_scale_to_f32<<<gs, NT, 0, st>>>(kd, nk, norm ? sumd : nullptr, scale * inv_p, kf);
   PVD_LAUNCH_CHECK("k_scale_to_f32");
-  k_spec_x<<<gs, NT, 0, st>>>(kf, t1, k0, k1, k2, Ke[2], o[2], p.P[2], p.H, p.tw[2]);
+  k_spec_x<<<gs, NT, 0, st>>>(kf, t1, k0, k1, k2, Ke[2], o[2], 0, p.P[2], p.H, p.tw[2]);
   PVD_LAUNCH_CHECK("k_spec_x");
-  k_spec_y<<<gs, NT, 0, st>>>(t1, t2, k0, k1, Ke[1], o[1], p.P[1], p.H, p.tw[1]);
+  k_spec_y<<<gs, NT, 0, st>>>(t1, t2, k0, k1, Ke[1], o[1], 0, p.P[1], p.H, p.tw[1]);
   PVD_LAUNCH_CHECK("k_spec_y");
-  k_spec_z<<<gs, NT, 0, st>>>(t2, p.spec[0], smode, Ke[0], o[0], p.P[0], p.P[1], p.H, p.HS, p.tw[0]);
+  k_spec_z<<<gs, NT, 0, st>>>(t2, p.spec[0], smode, Ke[0], o[0], 0, p.P[0], p.P[1], p.H, p.HS, p.tw[0]);
   PVD_LAUNCH_CHECK("k_spec_z");
   // the array keeps the previous call's contents: the padding columns [H, HS)
   // of the first work buffer must start at zero

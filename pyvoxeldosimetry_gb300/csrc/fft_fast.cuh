@@ -190,6 +190,18 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), z_min_blocks(A, B)) kf_z(cons
 // bulk tensor copies need for their shared-memory destination.
 static_assert(FTX * sizeof(float2) % 128 == 0, "TMA stage rows must be multiples of 128 bytes");
 
+// Bounded wait of the whole CTA for a TMA stage's barrier phase.  On timeout every
+// thread learns of it and thread 0 records PVD_ERR_TIMEOUT in *err (read by
+// pvd_plan_status); the caller then leaves the kernel.
+__device__ __forceinline__ bool cta_stage_wait(uint64_t* bar, uint32_t parity, uint64_t limit_ns, int* err) {
+  const bool ok = mbar_wait_bounded(bar, parity, limit_ns);
+  if (__syncthreads_or(!ok)) {
+    if (threadIdx.x == 0) atomicExch(err, (int)PVD_ERR_TIMEOUT);
+    return false;
+  }
+  return true;
+}
+
 __device__ __forceinline__ void tma_issue_rows(float2* dst, const CUtensorMap* map, int c0, int c2_or_row,
                                                bool rows_on_dim1, int chunks, int boxr, uint64_t* bar) {
   fence_proxy_async_shared();
@@ -232,11 +244,7 @@ __global__ void __launch_bounds__(FTX* cmax(A, B)) kt_y(const __grid_constant__ 
     if (threadIdx.x == 0 && tn < total)
       tma_issue_rows(sm + (s ^ 1) * SR * FTX, &tin, (tn % ctiles) * FTX, slab0 + tn / ctiles, true, chunks, boxr,
                      &bar[s ^ 1]);
-    const bool ok = mbar_wait_bounded(&bar[s], (i >> 1) & 1, TMA_WAIT_NS);
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicExch(err, (int)PVD_ERR_TIMEOUT);
-      return;
-    }
+    if (!cta_stage_wait(&bar[s], (i >> 1) & 1, TMA_WAIT_NS, err)) return;
     float2* stage = sm + s * SR * FTX;
     float2 v[B];
     if (j < A) {
@@ -291,11 +299,7 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), z_min_blocks(A, B)) kt_z(cons
     if (threadIdx.x == 0 && tn < total)
       tma_issue_rows(sm + (s ^ 1) * SR * FTX, &tin, (tn % ctiles) * FTX, tn / ctiles, false, chunks, boxr,
                      &bar[s ^ 1]);
-    const bool ok = mbar_wait_bounded(&bar[s], (i >> 1) & 1, TMA_WAIT_NS);
-    if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) atomicExch(err, (int)PVD_ERR_TIMEOUT);
-      return;
-    }
+    if (!cta_stage_wait(&bar[s], (i >> 1) & 1, TMA_WAIT_NS, err)) return;
     float2* stage = sm + s * SR * FTX;
     const int kx0 = (t % ctiles) * FTX, ky = t / ctiles;
     const long long base = (long long)ky * HS + kx0 + c;

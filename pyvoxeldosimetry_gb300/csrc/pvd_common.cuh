@@ -17,6 +17,12 @@ pvd_status set_error(pvd_status st, const std::string& msg);
 pvd_status cuda_error(cudaError_t e, const char* what);
 void count_launch(int n = 1);
 
+// Failure-path checks behind pvd_wait_check: one small kernel that waits, through the
+// bounded wait of the plan's TMA passes or of the U-Net's tensor-core pipeline, on an
+// mbarrier phase that nothing completes, and records the timeout where those do.
+pvd_status plan_wait_check(pvd_plan* p, unsigned long long limit_ns, cudaStream_t st);
+pvd_status unet_wait_check(unsigned long long limit_ns, cudaStream_t st);
+
 #define PVD_CUDA_TRY(expr)                                        \
   do {                                                            \
     cudaError_t _e = (expr);                                      \

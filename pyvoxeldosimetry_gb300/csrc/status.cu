@@ -44,3 +44,11 @@ extern "C" uint64_t pvd_launch_count(int reset) {
   if (reset) pvd::g_launches = 0;
   return v;
 }
+
+extern "C" pvd_status pvd_wait_check(int which, pvd_plan* plan, unsigned long long limit_ns, pvd_stream stream) {
+  if (limit_ns == 0 || limit_ns > 2000000000ull)
+    return pvd::set_error(PVD_ERR_ARG, "pvd_wait_check: limit_ns must be in (0, 2e9]");
+  if (which == PVD_WAITCHECK_PLAN) return pvd::plan_wait_check(plan, limit_ns, (cudaStream_t)stream);
+  if (which == PVD_WAITCHECK_UNET) return pvd::unet_wait_check(limit_ns, (cudaStream_t)stream);
+  return pvd::set_error(PVD_ERR_ARG, "pvd_wait_check: unknown target");
+}

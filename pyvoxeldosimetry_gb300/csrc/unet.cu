@@ -1476,6 +1476,31 @@ extern "C" pvd_status pvd_adam_step(float* params, const float* grads, float* m,
   return PVD_OK;
 }
 
+namespace pvd {
+namespace {
+// One warp waits, through the pipeline's own warp-wide bounded wait, on a barrier
+// phase that nothing completes (no bulk copy or MMA is issued), and records the
+// timeout like the load warp does.
+__global__ void k_unet_wait_check(uint64_t limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (!umma::warp_wait(&bar, 0, limit_ns)) {
+    if ((threadIdx.x & 31) == 0) fail(ST_TIMEOUT_LOAD);
+  }
+}
+}  // namespace
+
+pvd_status unet_wait_check(unsigned long long limit_ns, cudaStream_t st) {
+  k_unet_wait_check<<<1, 32, 0, st>>>(limit_ns);
+  PVD_LAUNCH_CHECK("k_unet_wait_check");
+  return PVD_OK;
+}
+}  // namespace pvd
+
 extern "C" pvd_status pvd_unet_status(int* code, int reset) {
   if (!code) return set_error(PVD_ERR_ARG, "pvd_unet_status: null output");
   PVD_CUDA_TRY(cudaMemcpyFromSymbol(code, g_unet_status, sizeof(int)));

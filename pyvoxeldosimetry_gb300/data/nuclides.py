@@ -26,6 +26,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import mc_decay
+
 JOULE_PER_MEV = 1.602176634e-13
 
 
@@ -45,19 +47,18 @@ class Nuclide:
 
 
 NUCLIDES = {
+    # Y-90's kernel half-life is data/dose_kernels/Y90/Y90.json's 64.1 h (the Monte Carlo
+    # data file says 64.053 h); spectra and gamma lines come from the Monte Carlo data
     "Y90": Nuclide("Y90", 64.1, 0.934, 2.280, 11.3, 15.0,
-                   spectrum_e=(0.0, 0.2, 0.4, 0.6, 0.8, 1.0, 1.2, 1.4, 1.6, 1.8, 2.0, 2.2, 2.280),
-                   spectrum_p=(0.0, 0.12, 0.22, 0.30, 0.36, 0.40, 0.42, 0.38, 0.32, 0.24, 0.15, 0.06, 0.0),
+                   spectrum_e=mc_decay.beta_spectrum("Y90")[0], spectrum_p=mc_decay.beta_spectrum("Y90")[1],
                    beta_branches=((2.280, 1.0),)),
-    "Lu177": Nuclide("Lu177", 6.647 * 24.0, 0.149, 0.498, 1.7, 6.0,
-                     spectrum_e=(0.0, 0.1, 0.2, 0.3, 0.4, 0.498),
-                     spectrum_p=(0.0, 0.35, 0.48, 0.42, 0.22, 0.0),
-                     gammas=((0.208, 0.1094), (0.113, 0.0641)),
+    "Lu177": Nuclide("Lu177", mc_decay.half_life_hours("Lu177"), 0.149, 0.498, 1.7, 6.0,
+                     spectrum_e=mc_decay.beta_spectrum("Lu177")[0], spectrum_p=mc_decay.beta_spectrum("Lu177")[1],
+                     gammas=mc_decay.gamma_lines("Lu177"),
                      beta_branches=((0.498, 0.795), (0.385, 0.089), (0.177, 0.116))),
-    "I131": Nuclide("I131", 8.0207 * 24.0, 0.182, 0.807, 3.2, 7.5,
-                    spectrum_e=(0.0, 0.1, 0.2, 0.3, 0.4, 0.5, 0.6, 0.7, 0.807),
-                    spectrum_p=(0.0, 0.25, 0.42, 0.48, 0.42, 0.32, 0.20, 0.08, 0.0),
-                    gammas=((0.364, 0.812), (0.637, 0.0717), (0.284, 0.0606))),
+    "I131": Nuclide("I131", mc_decay.half_life_hours("I131"), 0.182, 0.807, 3.2, 7.5,
+                    spectrum_e=mc_decay.beta_spectrum("I131")[0], spectrum_p=mc_decay.beta_spectrum("I131")[1],
+                    gammas=mc_decay.gamma_lines("I131")),
     "F18": Nuclide("F18", 1.8295, 0.250, 0.634, 2.4, 6.0),
     "Ga68": Nuclide("Ga68", 1.128, 0.836, 1.899, 9.0, 12.0),
     "Tb161": Nuclide("Tb161", 165.432, 0.154, 0.593, 1.8, 6.0),

@@ -1,7 +1,7 @@
 """Generate golden vectors by running the reference implementation itself.
 
-Imports devhliu/PyVoxelDosimetry from a read-only checkout (default
-/root/reference, override with PVD_REFERENCE) and records inputs/outputs of
+Imports devhliu/PyVoxelDosimetry from a read-only checkout (the directory named
+by the PVD_REFERENCE environment variable) and records inputs/outputs of
 the functions on the dose hot path into ``reference_golden.npz`` next to this
 file.  The GPU machine has no reference checkout: the committed .npz is what the
 tests read there.
@@ -20,6 +20,8 @@ Recorded (reference file:line in parentheses):
   adv_*    TimeCurveFitting.fit_time_activity_curve_advanced (curve_fitting.py:112-219)
   y90k_*   Y90KernelGenerator.generate_kernel (data/dose_kernels/y90_kernel.py:20-55)
   dvh_*    calculate_dvh (core/utils.py:233-262)
+  tissue_* TissueComposition.calculate_composition (tissue/composition.py:48-93)
+  reference_mc_decay.json: load_decay_data (data/mc_decay/__init__.py:10-24) of Y90, Lu177, I131
   kgen_*   Ga68KernelGenerator.generate_kernel (data/dose_kernels/ga68_kernel.py:19-106),
            Lu177KernelGenerator.generate_kernel (lu177_kernel.py:52-184), and the
            alpha / gamma terms of Ac225KernelGenerator (ac225_kernel.py:140-184; its
@@ -27,7 +29,7 @@ Recorded (reference file:line in parentheses):
            JSON files carry // comments, which json.load rejects; they are read with
            the comments stripped.
 
-Run:  python tests/golden/make_golden.py
+Run:  PVD_REFERENCE=<checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -39,8 +41,9 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path(os.environ.get("PVD_REFERENCE", "/root/reference"))
+REF = Path(os.environ["PVD_REFERENCE"]) if "PVD_REFERENCE" in os.environ else None
 OUT = Path(__file__).resolve().parent / "reference_golden.npz"
+DECAY_OUT = Path(__file__).resolve().parent / "reference_mc_decay.json"
 
 
 class _Stub(types.ModuleType):
@@ -89,6 +92,8 @@ def strip_json_comments(text: str) -> str:
 
 
 def main():
+    if REF is None or not (REF / "pyvoxeldosimetry").is_dir():
+        raise SystemExit("set PVD_REFERENCE to a checkout of devhliu/PyVoxelDosimetry")
     sys.dont_write_bytecode = True
     _install_stubs()
     sys.path.insert(0, str(REF))
@@ -238,8 +243,46 @@ def main():
                                                                                      gl["intensity"])
                                                    for gl in ac.gamma_lines])
 
+    # ---- convolution on shapes with prime factors > 7 (own generator: the vectors above stay) ----
+    r3 = np.random.default_rng(1117)
+    prime_cases = {
+        "prime_small": ((11, 13, 17), (5, 5, 5)),
+        "prime_mixed": ((37, 16, 43), (7, 9, 5)),
+        "prime_oversize": ((5, 7, 11), (9, 9, 13)),   # kernel truncated to A.shape
+        "prime_thin": ((1, 23, 29), (1, 3, 3)),
+    }
+    for name, (shape, kshape) in prime_cases.items():
+        a = r3.random(shape) * 100.0
+        k = r3.random(kshape)
+        g[f"conv_{name}_A"] = a
+        g[f"conv_{name}_K"] = k
+        g[f"conv_{name}_D"] = conv_calc(k).calculate_dose_rate(a, (1.0, 1.0, 1.0))
+
+    # ---- tissue composition from HU, with and without the metal-artefact step ----
+    from pyvoxeldosimetry.tissue.composition import TissueComposition
+    r4 = np.random.default_rng(4242)
+    for name, shape in (("odd", (14, 17, 19)), ("thin", (3, 40, 33))):
+        ct = np.round(r4.uniform(-1100.0, 3600.0, shape))
+        edges = [-1000, -900, -500, -100, 100, 300, 3000, -10, 10, 2000, 2001]
+        flat = ct.reshape(-1)
+        flat[:len(edges)] = edges                       # values on every range boundary
+        flat[len(edges)] = np.nan
+        ct[0, :2, :3] = 2500.0                          # metal on the boundary (reflect)
+        ct[shape[0] // 2, 5:9, 6:10] = 3200.0           # a metal block
+        for art in (True, False):
+            comp = TissueComposition().calculate_composition(ct.copy(), handle_artifacts=art)
+            for t, m in comp.items():
+                g[f"tissue_{name}_{int(art)}_{t}"] = m
+        g[f"tissue_{name}_ct"] = ct
+
     np.savez_compressed(OUT, **g)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")
+
+    # ---- Monte Carlo decay data as the reference loads it (data/mc_decay/__init__.py:10-24) ----
+    from pyvoxeldosimetry.data.mc_decay import load_decay_data
+    decay = {n: load_decay_data(n) for n in ("Y90", "Lu177", "I131")}
+    DECAY_OUT.write_text(json.dumps(decay, indent=1, sort_keys=True) + "\n")
+    print(f"wrote {DECAY_OUT}")
 
 
 if __name__ == "__main__":

@@ -46,18 +46,33 @@ def radial_kernel(k, lam=1.8, dx=2.0):
     return np.exp(-r / lam) / r ** 2
 
 
-@pytest.mark.parametrize("name", ["ragged_asym", "cube_radial", "oversize", "even_kernel", "thin"])
+CONV_CASES = ["ragged_asym", "cube_radial", "oversize", "even_kernel", "thin",
+              "prime_small", "prime_mixed", "prime_oversize", "prime_thin"]
+
+
+@pytest.mark.parametrize("name", CONV_CASES)
 def test_reference_circular_matches_reference_golden(golden, name):
+    """Every shape, including dims with prime factors > 7 (11, 13, 17, 23, 29, 37, 43):
+    those axes run at a padded length >= 2n with the kernel's image copy."""
     a = golden[f"conv_{name}_A"]
     k = golden[f"conv_{name}_K"]
     ref = golden[f"conv_{name}_D"]          # produced by the reference's own calculate_dose_rate
-    try:
-        d = run_plan(a, [k], mode="reference_circular")[0]
-    except Exception as e:  # dims with a prime factor > 7 are not supported in circular mode
-        from pyvoxeldosimetry_gb300._native import PvdError
-        assert isinstance(e, PvdError) and "7-smooth" in str(e)
-        pytest.skip(str(e))
+    d = run_plan(a, [k], mode="reference_circular")[0]
     assert rel_err(d, ref) <= TOL
+
+
+def test_reference_circular_explicit_pads():
+    """An explicit pad of n (7-smooth) or of any 7-smooth length >= 2n gives the same
+    period-n result; lengths in between are rejected."""
+    from pyvoxeldosimetry_gb300._native import PvdError
+    rng = np.random.default_rng(41)
+    a = rng.random((12, 10, 14))
+    k = rng.random((5, 3, 7))
+    ref = oc.reference_circular_conv(a, k)
+    for pad in [(12, 10, 14), (24, 20, 28), (25, 27, 30), (12, 21, 14)]:
+        assert rel_err(run_plan(a, [k], mode="reference_circular", pad=pad)[0], ref) <= TOL
+    with pytest.raises(PvdError, match="at least 2n"):
+        run_plan(a, [k], mode="reference_circular", pad=(16, 10, 14))
 
 
 @pytest.mark.parametrize("shape,ks", [((17, 23, 29), (5, 5, 5)), ((32, 32, 32), (7, 7, 7)),
@@ -125,8 +140,8 @@ def test_config1_size_against_fp64_oracle():
 def test_errors_are_raised_not_faulted():
     from pyvoxeldosimetry_gb300._native import PvdError
     from pyvoxeldosimetry_gb300.conv import ConvPlan
-    with pytest.raises(PvdError):
-        ConvPlan((11, 13, 17), kmax=(3, 3, 3), mode="reference_circular")  # 11, 13, 17 not 7-smooth
+    with pytest.raises(PvdError, match="UNSUPPORTED"):
+        ConvPlan((1031, 8, 8), kmax=(3, 3, 3), mode="reference_circular")  # prime 1031: length >= 2062
     with ConvPlan((8, 8, 8), kmax=(3, 3, 3)) as p:
         with pytest.raises(PvdError, match="STATE"):
             p.execute(torch.zeros((8, 8, 8), device="cuda"))

@@ -7,7 +7,11 @@ from oracle import conv as oc
 from oracle import time_fit as of
 
 
-@pytest.mark.parametrize("name", ["ragged_asym", "cube_radial", "oversize", "even_kernel", "thin"])
+CONV_CASES = ["ragged_asym", "cube_radial", "oversize", "even_kernel", "thin",
+              "prime_small", "prime_mixed", "prime_oversize", "prime_thin"]
+
+
+@pytest.mark.parametrize("name", CONV_CASES)
 def test_circular_conv_is_reference(golden, name):
     d = oc.reference_circular_conv(golden[f"conv_{name}_A"], golden[f"conv_{name}_K"])
     np.testing.assert_allclose(d, golden[f"conv_{name}_D"], rtol=0, atol=1e-12 * np.abs(d).max())
@@ -159,3 +163,40 @@ def test_multi_kernel_oracle_equals_single_kernel_oracle():
         np.testing.assert_allclose(d, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
     st = oc.error_stats(outs[0] * (1 + 1e-6), outs[0])
     assert 0.9e-6 < st["max_normwise"] < 1.1e-6 and st["mean_normwise"] <= st["max_normwise"]
+
+
+def _image_copy_circular(a, k, pads):
+    """The GPU plan's method for CIRCULAR axes of any length, restated in numpy: per axis a
+    length P (P == n, or P >= 2n), the kernel (truncated to n) at the corner and, when
+    P > n, a second copy at offset P - n; zero-padded input; keep the first n outputs."""
+    kp = np.zeros(pads)
+    kt = k[tuple(slice(0, min(kk, n)) for kk, n in zip(k.shape, a.shape))]
+    offs = [(0,) if P == n else (0, P - n) for P, n in zip(pads, a.shape)]
+    for o0 in offs[0]:
+        for o1 in offs[1]:
+            for o2 in offs[2]:
+                kp[o0:o0 + kt.shape[0], o1:o1 + kt.shape[1], o2:o2 + kt.shape[2]] += kt
+    full = np.fft.ifftn(np.fft.fftn(a, pads) * np.fft.fftn(kp)).real
+    return full[:a.shape[0], :a.shape[1], :a.shape[2]]
+
+
+@pytest.mark.parametrize("name", CONV_CASES)
+def test_circular_by_image_copy_equals_reference(golden, name):
+    """Any P >= 2n with the kernel's image copy reproduces the reference's period-n
+    operator, also when only some axes are padded."""
+    a, k = golden[f"conv_{name}_A"], golden[f"conv_{name}_K"]
+    ref = golden[f"conv_{name}_D"]
+    for pads in (tuple(2 * n for n in a.shape), tuple(2 * n + 3 for n in a.shape),
+                 (a.shape[0], 2 * a.shape[1] + 1, a.shape[2])):
+        d = _image_copy_circular(a, k, pads)
+        np.testing.assert_allclose(d, ref, rtol=0, atol=1e-12 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("name", ["odd", "thin"])
+@pytest.mark.parametrize("art", [0, 1])
+def test_tissue_composition_oracle_is_reference(golden, name, art):
+    from oracle import tissue as ot
+    ct = golden[f"tissue_{name}_ct"]
+    comp = ot.composition(ct, artifacts=bool(art))
+    for t, m in comp.items():
+        np.testing.assert_array_equal(m, golden[f"tissue_{name}_{art}_{t}"])
