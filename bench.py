@@ -697,17 +697,23 @@ def batch_volumes(device, n_volumes=64, seed=3, times=(1.0, 4.0, 24.0, 96.0), n_
     return vols
 
 
-def measure_batch(device, n_volumes=8, reps=2):
-    """Batched time-integrated dose: per-voxel two-exponential fit (variable projection,
-    FP32 iterations finished in FP64) + analytic AUC + Y-90 convolution of every volume,
-    recorded once as a CUDA graph and launched as one."""
+def measure_batch(device, n_volumes=64, reps=2):
+    """Batched time-integrated dose of the seeded uneven workload: per-voxel two-exponential
+    fit (variable projection: FP32 iterations, FP64 Gauss-Newton polish, FP64 trust region
+    for what the polish leaves) + analytic AUC + Y-90 convolution at autotuned FFT lengths
+    of every volume, recorded once as a CUDA graph and launched as one.  The stages are
+    also timed apart (every fit, then every convolution) for the fit's Mvoxel/s and the
+    convolution stage's HBM fraction."""
     import torch
     from pyvoxeldosimetry_gb300 import _native as N
     from pyvoxeldosimetry_gb300.batch import BatchDoseCalculator
+    from pyvoxeldosimetry_gb300.data import nuclides as nd
+    t0 = time.perf_counter()
     vols = batch_volumes(device, n_volumes)
     nvox = sum(int(np.prod(v["activity"].shape[1:])) for v in vols)
-    bc = BatchDoseCalculator("Y90", use_graph=True, device=device)
+    bc = BatchDoseCalculator("Y90", use_graph=True, autotune=True, device=device)
     bc.prepare(vols)
+    setup_s = time.perf_counter() - t0
     lib = N.load()
     ms = []
     for _ in range(reps + 1):
@@ -719,17 +725,25 @@ def measure_batch(device, n_volumes=8, reps=2):
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
     launches = int(lib.pvd_launch_count(1))
+    fit_ms, conv_ms = bc.run_stages()
     ok = float(sum(float(bc.fit_results(i)[2].float().mean()) * np.prod(v["activity"].shape[1:])
                    for i, v in enumerate(vols)) / nvox)
+    peak, _ = load_peaks()
+    ks = nd.default_kernel_size("Y90", (1.5, 1.5, 1.5))
+    conv_bytes = sum(byte_model(tuple(v["activity"].shape[1:]), ks, 1, False)["_per_step"] for v in vols)
+    lengths = sorted({tuple(p.fft_shape) for p in bc.plans()})
     bc.close()
     del vols
     torch.cuda.empty_cache()
     t = float(np.median(ms[1:]))
     return {"value": nvox / (t / 1e3) / 1e9, "unit": "Gvoxel/s", "ms_per_batch": t, "volumes": n_volumes,
             "voxels": nvox, "gpu_launches_per_batch": launches, "fit_converged_fraction": ok,
-            "workload": f"{n_volumes} volumes 96..320 x 96..320 x 96..256 at 1.5 mm, 4 timepoints, Y-90 21^3, "
-                        "one graph launch (default FFT lengths, autotuner off)",
-            "sample": f"the first {n_volumes} of 64 seeded volume shapes"}
+            "fit_ms": fit_ms, "fit_mvoxel_s": nvox / (fit_ms / 1e3) / 1e6,
+            "conv_ms": conv_ms, "conv_gvoxel_s": nvox / (conv_ms / 1e3) / 1e9,
+            "conv_hbm_frac": conv_bytes / (conv_ms / 1e3) / 1e9 / peak, "conv_algorithmic_bytes": conv_bytes,
+            "distinct_fft_shapes": len(lengths), "setup_s": setup_s,
+            "workload": f"{n_volumes} seeded volumes 96..320 x 96..320 x 96..256 at 1.5 mm, 4 timepoints (1, 4, 24, "
+                        "96 h), Y-90 21^3, autotuned FFT lengths per volume shape, one graph launch"}
 
 
 def config_dict(name, wl):
@@ -752,7 +766,7 @@ def main():
     ap.add_argument("--no-check", action="store_true", help="skip the error check against the FP64 oracle")
     ap.add_argument("--pads", help="explicit FFT lengths P0,P1,P2 (default: the autotuner's choice)")
     ap.add_argument("--no-extras", action="store_true", help="skip the MC, fit and batch sub-measurements")
-    ap.add_argument("--batch-volumes", type=int, default=8,
+    ap.add_argument("--batch-volumes", type=int, default=64,
                     help="volumes of the 64-volume seeded uneven batch to run in the batch sub-measurement")
     ap.add_argument("--only", choices=["mc", "fit", "vpfit", "batch", "dvh", "resample", "unet"],
                     help="run one sub-measurement alone and print it (no contract line)")

@@ -136,8 +136,8 @@ pvd_status pvd_conv_execute(pvd_plan* plan, const float* activity_d, const float
  * dose_h are host float32 arrays of the sizes above.  The plan stages them in
  * device buffers it owns and pipelines the copies with the passes: the
  * activity goes up in z chunks that each release their share of the forward
- * passes, the density goes up during the z pass, and each slot's dose comes
- * back while the next slot computes.  Returns once queued; the copies back
+ * passes, the density goes up during the z pass, and the inverse x pass runs in
+ * z chunks whose dose (every slot's) goes back while the next chunk computes.  Returns once queued; the copies back
  * are complete when `stream` is (cudaStreamSynchronize).  Page-locked host
  * memory makes the copies asynchronous; pageable memory works but copies
  * synchronously. */
@@ -244,7 +244,11 @@ enum {
  * times the largest sample, and the integral finite;
  * otherwise the voxel is marked not ok and the model's own AUC rule is used).  PVD_FIT_MIXED runs the iterations in FP32, then the same minimiser
  * again in FP64 from where they stopped, with at most 60 evaluations; success
- * is decided by the FP64 run's convergence tests alone.  PVD_FIT_VARPRO (f4a only) minimises the same
+ * is decided by the FP64 run's convergence tests alone.  With PVD_FIT_VARPRO
+ * the FP64 run starts with at most three Gauss-Newton steps from the FP32
+ * rates; a voxel whose curve then reproduces its float32 samples to their
+ * rounding (the FP64 run's own stopping test) is done, and only the others go
+ * through the FP64 trust-region iteration.  PVD_FIT_VARPRO (f4a only) minimises the same
  * least-squares cost by variable projection: the two amplitudes are solved
  * linearly for given rates and the trust-region iteration runs over the two
  * rates only, which converges where the four-parameter iteration stalls in the
@@ -636,6 +640,19 @@ pvd_status pvd_unet_bias_grad(const pvd_unet_geom* geom, const void* grad, int c
 /* Adam (bias-corrected, decoupled weight decay) on n FP32 parameters; step >= 1. */
 pvd_status pvd_adam_step(float* params, const float* grads, float* m, float* v, int64_t n, float lr, float beta1,
                          float beta2, float eps, float weight_decay, int step, pvd_stream stream);
+
+/* Global-norm gradient clipping before pvd_adam_step: norm = ||grads||_2 over n
+ * FP32 values (fixed-order reduction, FP64 partial sums), then grads *= min(1,
+ * max_norm / norm).  The gradients are zeroed (the step is then carried by
+ * Adam's moments alone, which the outlier does not enter) when the norm is not
+ * finite or, with spike_factor > 0, exceeds spike_factor times the running mean
+ * of the norms accepted so far.  work: device float32 of PVD_GRAD_CLIP_WORK
+ * values, zeroed before the first step and kept between steps: work[1024]
+ * receives the norm, work[1025] the scale, work[1026] holds the running mean,
+ * work[1027] counts the dropped steps.  No host round trip. */
+#define PVD_GRAD_CLIP_WORK 1028
+pvd_status pvd_grad_clip(float* grads, int64_t n, float max_norm, float spike_factor, float* work,
+                         pvd_stream stream);
 
 /* First failure code recorded by a U-Net kernel (0: none; a bounded wait of
  * the tensor-core pipeline ran out otherwise, and PVD_ERR_TIMEOUT is

@@ -49,7 +49,7 @@ EXPORTED_SYMBOLS = [
     "pvd_unet_geometry", "pvd_unet_conv3d", "pvd_unet_wgrad_workspace", "pvd_unet_conv3d_wgrad",
     "pvd_unet_pack_weights", "pvd_unet_pack_input", "pvd_unet_pool", "pvd_unet_pool_backward",
     "pvd_unet_upsample", "pvd_unet_upsample_backward", "pvd_unet_head", "pvd_unet_head_loss_workspace",
-    "pvd_unet_head_loss", "pvd_unet_apply_correction", "pvd_unet_input_maxima", "pvd_unet_bias_grad_workspace", "pvd_unet_bias_grad", "pvd_adam_step",
+    "pvd_unet_head_loss", "pvd_unet_apply_correction", "pvd_unet_input_maxima", "pvd_unet_bias_grad_workspace", "pvd_unet_bias_grad", "pvd_adam_step", "pvd_grad_clip",
     "pvd_unet_status",
     "pvd_wait_check", "pvd_set_plan_alloc_cap",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
@@ -197,6 +197,7 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_unet_bias_grad_workspace": (st, [C.POINTER(UnetGeom), i, C.POINTER(C.c_size_t)]),
         "pvd_unet_bias_grad": (st, [C.POINTER(UnetGeom), vp, i, vp, vp, C.c_size_t, vp]),
         "pvd_adam_step": (st, [vp, vp, vp, vp, C.c_int64, f, f, f, f, f, i, vp]),
+        "pvd_grad_clip": (st, [vp, C.c_int64, f, f, vp, vp]),
         "pvd_unet_status": (st, [C.POINTER(i), i]),
         "pvd_wait_check": (st, [i, vp, C.c_ulonglong, vp]),
         "pvd_set_plan_alloc_cap": (st, [C.c_size_t]),

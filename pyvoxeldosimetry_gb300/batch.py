@@ -34,6 +34,23 @@ from .data import nuclides as nd
 SECONDS_PER_HOUR = 3600.0
 
 
+def partition_volumes(shapes: Sequence[Sequence[int]], world: int) -> List[List[int]]:
+    """Volumes of a batch shared out over ``world`` replicas (one GPU each): largest
+    first, each to the replica with the fewest voxels so far (ties to the lower rank),
+    so every rank computes the same assignment without communicating.  Returns, per
+    rank, the indices of its volumes in ascending order."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    sizes = [int(np.prod(s)) for s in shapes]
+    load = [0] * world
+    parts: List[List[int]] = [[] for _ in range(world)]
+    for i in sorted(range(len(sizes)), key=lambda k: (-sizes[k], k)):
+        r = min(range(world), key=lambda k: (load[k], k))
+        parts[r].append(i)
+        load[r] += sizes[i]
+    return [sorted(x) for x in parts]
+
+
 class BatchDoseCalculator:
     def __init__(self, radionuclide: str = "Y90", kernel_size=None, use_graph: bool = True, mixed_fit: bool = True,
                  autotune: bool = False, max_fev: int = 2000, device=None):
@@ -141,6 +158,35 @@ class BatchDoseCalculator:
                 N.check(self._lib.pvd_batch_execute(self._desc, len(self._items), self._fit_flags(),
                                                     self.max_fev, SECONDS_PER_HOUR, sh))
         return [it["dose"][0] for it in self._items]
+
+    def run_stages(self):
+        """The batch's work as two directly enqueued stages, every volume's fit and then
+        every volume's convolution, with CUDA events around each stage (instrumentation
+        for measuring the stages apart; ``run`` is the production call).  Returns
+        (fit_ms, conv_ms)."""
+        if not self._items:
+            return 0.0, 0.0
+        p0 = (C.c_double * 5)(1.0, 0.1, 0.5, 0.01, 0.0)
+        flags = self._fit_flags() | N.PVD_FIT_P0_FROM_DATA | N.PVD_FIT_AUC_INF
+        with torch.cuda.device(self.device):
+            st = torch.cuda.current_stream(self.device)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            ev[0].record(st)
+            for it in self._items:
+                N.check(self._lib.pvd_tac_fit(N.PVD_FIT_F4A, it["times_c"], None, len(it["times"]), p0, 0.0, 0.0,
+                                              self.max_fev, flags, it["act"].data_ptr(), it["nvox"],
+                                              it["params"].data_ptr(), it["auc"].data_ptr(), it["ok"].data_ptr(),
+                                              it["cum"].data_ptr(), SECONDS_PER_HOUR, st.cuda_stream))
+            ev[1].record(st)
+            for it in self._items:
+                it["plan"].execute(it["cum"], density=it["rho"], out=it["dose"], stream=st)
+            ev[2].record(st)
+            ev[2].synchronize()
+        return ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+
+    def plans(self):
+        """The convolution plan of each volume, in order."""
+        return [it["plan"] for it in self._items]
 
     def calculate(self, volumes: Sequence[dict]) -> List[torch.Tensor]:
         self.prepare(volumes)

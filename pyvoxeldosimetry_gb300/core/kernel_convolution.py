@@ -24,6 +24,9 @@ Differences from the reference, each deliberate:
     activity's grid (``config['resample_output'] = 'kernel'`` returns the
     kernel-grid dose, which is what the reference's stub was meant to feed);
   * an optional density map gives the density-scaled dose D/rho;
+  * ``config['energy_per_decay_mev']`` (a number or {nuclide: number}) replaces the
+    stated mean beta energy the analytic kernel is normalised to (the learned
+    correction uses the mean of the spectrum its Monte Carlo samples);
   * the multi-timepoint trapezoid runs as ONE convolution of the trapezoid-
     weighted activity (identical by linearity) with the weighting fused into
     the first FFT pass;
@@ -106,7 +109,9 @@ class KernelConvolutionCalculator(DosimetryCalculator):
         for nuc in self.nuclides:
             shape = self._size_for(nuc, vs if self.kernel_profile == "analytic" else self.kernel_resolution)
             if self.kernel_profile == "analytic":
-                specs.append((nd.analytic_profile(nuc, vs, shape), nd.gy_per_bq_s_scale(nuc, vs), True))
+                e = self.config.get("energy_per_decay_mev")
+                e = e.get(nuc) if isinstance(e, dict) else e
+                specs.append((nd.analytic_profile(nuc, vs, shape), nd.gy_per_bq_s_scale(nuc, vs, energy_mev=e), True))
             else:
                 specs.append((nd.reference_profile(nuc, self.tissue_name, float(self.kernel_resolution), shape),
                               1.0, False))
@@ -115,7 +120,7 @@ class KernelConvolutionCalculator(DosimetryCalculator):
     def _plan_for(self, shape, voxel_size, device) -> ConvPlan:
         vs = tuple(float(v) for v in voxel_size)
         spec_key = (vs, id(self.kernel), self.kernel_profile, repr(self.kernel_size), self.tissue_name,
-                    float(self.kernel_resolution))
+                    float(self.kernel_resolution), repr(self.config.get("energy_per_decay_mev")))
         key = (tuple(shape), self.mode, str(device), spec_key)
         if self._plan is not None and self._plan_key == key:
             return self._plan

@@ -160,6 +160,8 @@ class TrainStats:
     seconds: float = 0.0
     loss_mu: List[float] = field(default_factory=list)
     loss_s: List[float] = field(default_factory=list)
+    grad_norm: List[float] = field(default_factory=list)  # before clipping
+    skipped: int = 0                                      # steps dropped as gradient spikes
 
 
 class UNet3D:
@@ -190,6 +192,7 @@ class UNet3D:
         self.v = torch.zeros(self.n_params, dtype=torch.float32, device=self.device)
         self.packed_fwd = torch.zeros(po, dtype=torch.bfloat16, device=self.device)
         self.packed_bwd = torch.zeros(po, dtype=torch.bfloat16, device=self.device)
+        self.clip_work = torch.zeros(1028, dtype=torch.float32, device=self.device)
         self.step = 0
         self._ws: Dict[Tuple[Tuple[int, int, int], bool], _Workspace] = {}
         self._packed_for = -1
@@ -349,6 +352,17 @@ class UNet3D:
         self._dgrad("e0b", gr["e0b"], gr["e0a"], t["e0a"], stream)
         self._wgrad("e0a", t["x0"], gr["e0a"], ws, stream)
 
+    def clip_gradients(self, max_norm: float, spike_factor: float = 0.0, stream=None) -> None:
+        """Scale the parameter gradients to a global L2 norm of at most max_norm, and drop
+        them when the norm exceeds spike_factor times the running mean of earlier norms
+        (on the device; the norm before clipping is left in clip_work[1024], the count of
+        dropped steps in clip_work[1027])."""
+        N.check(self._lib.pvd_grad_clip(self.grads.data_ptr(), self.n_params, float(max_norm), float(spike_factor),
+                                        self.clip_work.data_ptr(), _stream_handle(stream)))
+
+    def skipped_steps(self) -> int:
+        return int(self.clip_work[1027].item())
+
     def adam(self, lr: float = 1e-3, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8,
              weight_decay: float = 0.0, stream=None) -> None:
         self.step += 1
@@ -424,17 +438,31 @@ def make_pair(activity: np.ndarray, density: np.ndarray, dose_conv: np.ndarray, 
                         input_scales(float(np.max(activity)), dmax))
 
 
+def mc_consistent_config(radionuclide: str) -> dict:
+    """Convolution options under which the plain dose and the Monte Carlo emit the same
+    energy per decay: the analytic kernel is normalised to the mean energy of the beta
+    spectrum the Monte Carlo samples (the piecewise-linear density through the decay
+    data's spectrum points: 1.135 MeV for Y-90, 0.234 for Lu-177, 0.349 for I-131,
+    where the data files state means of 0.934, 0.149 and 0.182 MeV).  Without this the
+    ratio D_MC / D_conv carries that constant factor besides the heterogeneity the
+    network is meant to learn."""
+    from ..data.mc_physics import spectrum_mean
+    return {"energy_per_decay_mev": spectrum_mean(radionuclide)}
+
+
 def generate_training_pairs(n: int, shape=(64, 64, 64), voxel_mm: float = 4.0, radionuclide: str = "Y90",
                             histories: int = 20_000_000, seed: int = 100, rel_threshold: float = 0.1,
                             device=None) -> List[TrainingPair]:
     """Seeded CT-like phantoms -> (activity, density, density-scaled convolution
-    dose, Monte Carlo dose) on the GPU.  Both doses are dose rates (Gy/s)."""
+    dose, Monte Carlo dose) on the GPU.  Both doses are dose rates (Gy/s), the
+    convolution's normalised to the Monte Carlo's energy per decay
+    (``mc_consistent_config``)."""
     from ..phantoms import ct_phantom
     from .kernel_convolution import KernelConvolutionCalculator
     from .monte_carlo import MonteCarloCalculator
 
     dev = _require_cuda(device)
-    conv = KernelConvolutionCalculator(radionuclide)
+    conv = KernelConvolutionCalculator(radionuclide, config=mc_consistent_config(radionuclide))
     mc = MonteCarloCalculator(radionuclide, n_particles=histories)
     vox = (voxel_mm,) * 3
     pairs = []
@@ -453,9 +481,15 @@ def generate_training_pairs(n: int, shape=(64, 64, 64), voxel_mm: float = 4.0, r
 
 
 def train(net: UNet3D, pairs: Sequence[TrainingPair], steps: int, crop=(32, 32, 32), lr: float = 2e-3,
-          seed: int = 0, log_every: int = 0) -> TrainStats:
-    """Adam (cosine-decayed learning rate) on random crops of random pairs; a crop
-    lies inside its volume when it fits, else covers it from a random offset."""
+          seed: int = 0, log_every: int = 0, clip: float = 1.0, warmup: float = 0.05,
+          spike_factor: float = 10.0) -> TrainStats:
+    """Adam on random crops of random pairs; a crop lies inside its volume when it
+    fits, else covers it from a random offset.  The learning rate rises linearly over
+    the first ``warmup`` fraction of the steps, then decays on a cosine; gradients are
+    clipped to a global norm of ``clip`` (0: no clipping), and a step whose gradient
+    norm exceeds ``spike_factor`` times the running mean of the earlier ones is dropped
+    before it reaches Adam's moments: one outlying crop would otherwise throw the
+    moments and the weights off course."""
     rng = np.random.default_rng(seed)
     ws = net.workspace(crop, train=True)
     stream = _stream_handle(None)
@@ -469,15 +503,20 @@ def train(net: UNet3D, pairs: Sequence[TrainingPair], steps: int, crop=(32, 32, 
         net.pack_input(ws, (p.activity, p.density, p.dose_conv), p.scales, origin, stream)
         net.forward(ws, stream)
         net.backward(ws, p.target, p.weight, origin, stream)
-        lr_t = lr * 0.5 * (1 + math.cos(math.pi * it / max(1, steps)))
+        nw = max(1, int(warmup * steps))
+        lr_t = lr * (it + 1) / nw if it < nw else lr * 0.5 * (1 + math.cos(math.pi * (it - nw) / max(1, steps - nw)))
+        if clip > 0:
+            net.clip_gradients(clip, spike_factor if it >= nw else 0.0)
         net.adam(lr=lr_t)
         if log_every and (it % log_every == 0 or it == steps - 1):
             lm, ls = net.losses()
             stats.loss_mu.append(lm)
             stats.loss_s.append(ls)
+            stats.grad_norm.append(float(net.clip_work[1024]))
     torch.cuda.synchronize(net.device)
     stats.seconds = time.perf_counter() - t0
     stats.steps = steps
+    stats.skipped = net.skipped_steps()
     net.status()
     return stats
 
@@ -546,16 +585,20 @@ class NNCorrectedDoseCalculator(DosimetryCalculator):
     (core/dosimetry_base.py:8-70).  config: ``model`` (a UNet3D) or
     ``model_path`` (.npz from save_model), ``sigma_max`` (fallback threshold on
     the predicted error of log(D_MC/D_conv), default 0.5), plus the
-    convolution calculator's own options.  Without a density map the plain
-    convolution is returned: the correction is a correction for heterogeneity."""
+    convolution calculator's own options.  The convolution runs under
+    ``mc_consistent_config`` (the energy per decay of the Monte Carlo the network
+    was trained against) unless the config says otherwise.  Without a density map
+    the plain convolution is returned: the correction is a correction for
+    heterogeneity."""
 
     def __init__(self, radionuclide: str, tissue_composition=None, config: Optional[dict] = None):
         super().__init__(radionuclide, tissue_composition, config)
         if not isinstance(radionuclide, str):
             raise TypeError("NNCorrectedDoseCalculator takes one radionuclide")
         from .kernel_convolution import KernelConvolutionCalculator
+        conv_cfg = {**mc_consistent_config(radionuclide), **self.config}
         self.conv = KernelConvolutionCalculator(radionuclide, self.config.get("tissue_name", "water"),
-                                                self.config.get("kernel_resolution", 1.0), self.config)
+                                                self.config.get("kernel_resolution", 1.0), conv_cfg)
         model = self.config.get("model")
         if model is None and self.config.get("model_path"):
             model = load_model(self.config["model_path"], self.config.get("device"))

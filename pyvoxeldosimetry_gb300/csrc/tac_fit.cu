@@ -944,8 +944,63 @@ __device__ __forceinline__ void vp_store(const FitArgs& a, const VpVoxel<TM>& d,
   store_fit<M_F4A>(a, p, good, ymax, v, nvox, params, auc, ok, auc32);
 }
 
+// Marker in params[0] of a voxel that the FP64 polish left to the FP64 trust-region stage.
+constexpr int kVpPolished = 100;  // init code of a voxel the polish already stored
+
+// FP64 polish between the FP32 and the FP64 trust-region stages (PVD_FIT_MIXED): from
+// the FP32 rates, at most three Gauss-Newton steps on the two rates of the projected
+// problem (the same normal equations the trust region uses), each kept only if it
+// lowers the cost.  A voxel whose curve then reproduces its float32 samples to their
+// rounding (the FP64 stage's own stopping test, ||r|| <= fstop) is stored here; any
+// other keeps its FP32 rates in params[1], params[3] and gets NaN in params[0], which
+// sends it to the FP64 trust-region stage.  Near the minimum the Gauss-Newton steps
+// converge quadratically, and a warp runs them without the trust region's branches.
+template <int MV>
+__global__ void __launch_bounds__(kVpThreads) k_tac_fit_vp_polish(FitArgs a, const float* __restrict__ acts,
+                                                                  long long nvox, double* __restrict__ params,
+                                                                  double* __restrict__ auc,
+                                                                  unsigned char* __restrict__ ok,
+                                                                  float* __restrict__ auc32) {
+  constexpr int TM = ModelTraits<MV>::TMAX;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvox;
+       v += (long long)gridDim.x * blockDim.x) {
+    VpVoxel<TM> d;
+    vp_load<TM>(a, acts, nvox, v, d);
+    double lam[2] = {params[1 * nvox + v], params[3 * nvox + v]};
+    bool good = d.finite && a.T >= 4 && isfinite(lam[0]) && isfinite(lam[1]);
+    bool done = false;
+    if (good) {
+      double A[4], g[2];
+      double cost = vp_normal_eq<TM, double>(a, d.yw, lam, A, g);
+      for (int it = 0; it < 3 && isfinite(cost) && !done; ++it) {
+        if (sqrt(2.0 * cost) <= d.fstop) {
+          done = true;
+          break;
+        }
+        const double det = A[0] * A[3] - A[1] * A[1];
+        if (!(det > 0.0) || !isfinite(det)) break;
+        const double l1[2] = {lam[0] - (A[3] * g[0] - A[1] * g[1]) / det,
+                              lam[1] - (A[0] * g[1] - A[1] * g[0]) / det};
+        double A1[4], g1[2];
+        const double c1 = vp_normal_eq<TM, double>(a, d.yw, l1, A1, g1);
+        if (!(c1 < cost)) break;
+        lam[0] = l1[0], lam[1] = l1[1], cost = c1;
+        for (int i = 0; i < 4; ++i) A[i] = A1[i];
+        g[0] = g1[0], g[1] = g1[1];
+      }
+      if (!done && isfinite(cost) && sqrt(2.0 * cost) <= d.fstop) done = true;
+    }
+    if (done) {
+      vp_store<TM>(a, d, lam, true, v, nvox, params, auc, ok, auc32);
+    } else {
+      params[v] = (double)NAN;  // to the FP64 trust-region stage, from the FP32 rates
+    }
+  }
+}
+
 // STAGE 0: FP32 from the peeling start, rates handed over in params[1], params[3].
-// STAGE 1: FP64 from those rates (PVD_FIT_MIXED) or from the start, then the stores.
+// STAGE 1: FP64 from those rates (PVD_FIT_MIXED; only the voxels the polish left,
+// marked by NaN in params[0]) or from the start, then the stores.
 template <int MV, int STAGE>
 __global__ void __launch_bounds__(kVpThreads) k_tac_fit_vp(FitArgs a, const float* __restrict__ acts, long long nvox,
                                                            long long per_block, double* __restrict__ params,
@@ -965,6 +1020,7 @@ __global__ void __launch_bounds__(kVpThreads) k_tac_fit_vp(FitArgs a, const floa
   long long v = 0;
   auto init = [&](long long vv) -> int {
     v = vv;
+    if (STAGE == 1 && a.mixed && !isnan(params[v])) return kVpPolished;
     vp_load<TM>(a, acts, nvox, v, d);
     if (STAGE == 1 && a.mixed) {
       lam0[0] = params[1 * nvox + v];
@@ -983,6 +1039,7 @@ __global__ void __launch_bounds__(kVpThreads) k_tac_fit_vp(FitArgs a, const floa
   };
   auto tick = [&]() -> int { return lm_tick<MV, R>(a, yr, s); };
   auto finish = [&](int info) {
+    if (info == kVpPolished) return;
     if (STAGE == 0) {
       const bool f = isfinite(s.x[0]) && isfinite(s.x[1]);
       params[1 * nvox + v] = f ? (double)s.x[0] : lam0[0];
@@ -1043,12 +1100,15 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
     const long long nblk = std::min<long long>((n_vox + kVpThreads - 1) / kVpThreads, 152LL * 8);
     const long long per_block = (n_vox + nblk - 1) / nblk;
     const int g = (int)((n_vox + per_block - 1) / per_block);
+    const int pg = (int)std::min<long long>((n_vox + kVpThreads - 1) / kVpThreads, 152LL * 32);
 #define PVD_VP_LAUNCH(MV)                                                                                   \
   {                                                                                                         \
     if (a.mixed) {                                                                                          \
       k_tac_fit_vp<MV, 0><<<g, kVpThreads, 0, st>>>(a, acts_d, n_vox, per_block, params_d, auc_d, ok_d,     \
                                                     auc_f32_d);                                             \
       PVD_LAUNCH_CHECK("k_tac_fit_vp<fp32>");                                                               \
+      k_tac_fit_vp_polish<MV><<<pg, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d); \
+      PVD_LAUNCH_CHECK("k_tac_fit_vp_polish");                                                              \
     }                                                                                                       \
     k_tac_fit_vp<MV, 1><<<g, kVpThreads, 0, st>>>(a, acts_d, n_vox, per_block, params_d, auc_d, ok_d,       \
                                                   auc_f32_d);                                               \

@@ -331,7 +331,7 @@ constexpr int STK_OUT = STK_ROWS - 2;              // output rows per tile
 constexpr uint32_t STK_PITCH = STK_ROWS * 16;      // bytes of one plane's slab
 
 template <int CO>
-__global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3s(const ConvArgs a) {
+__global__ void __launch_bounds__(CONV_THREADS, CO == 16 ? 4 : 3) k_conv3s(const ConvArgs a) {
   extern __shared__ __align__(128) uint8_t sm[];
   const int cin8 = a.cin >> 3;
   constexpr int n3 = 3 * CO;
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3s(const ConvArgs a) {
   const int na = a.na;
   uint8_t* sa = sm;
   uint8_t* sb = sm + (size_t)na * a_bytes;
-  constexpr int xp = CO + 1;  // exchange row pitch (odd: no bank conflicts)
+  constexpr int xp = CO + 4;  // exchange row pitch: 16-byte rows, 8 consecutive rows on distinct banks
   float* xch = reinterpret_cast<float*>(sb + (size_t)9 * g_bytes);  // [2][128][cout + 1] exchange
   uint64_t* full_a = reinterpret_cast<uint64_t*>(xch + 2 * STK_ROWS * xp);
   uint64_t* empty_a = full_a + na;
@@ -349,6 +349,7 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3s(const ConvArgs a) {
   uint64_t* acc_empty = acc_full + 2;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(acc_empty + 2);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1);  // an epilogue warp timed out
+  float* bias_s = reinterpret_cast<float*>(tslot + 4);                    // [CO] bias (0 without one)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t ncols = umma::tmem_cols(2 * n3);
 
@@ -439,8 +440,10 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3s(const ConvArgs a) {
     const int q = warp & 3;
     const int r = 32 * q + lane;
     constexpr int co = CO;
-    float* x1 = xch;                 // [128][cout + 1]: P[.][1]
-    float* x2 = xch + STK_ROWS * xp; // [128][cout + 1]: P[.][2]
+    float* x1 = xch;                 // [128][cout + 4]: P[.][1]
+    float* x2 = xch + STK_ROWS * xp; // [128][cout + 4]: P[.][2]
+    if (r < CO) bias_s[r] = a.bias ? __ldg(a.bias + r) : 0.f;  // the bias, loaded once
+    asm volatile("bar.sync 1, 128;" ::: "memory");
     int t_local = 0;
     for (int tile = blockIdx.x; tile < a.n_tiles; tile += gridDim.x, ++t_local) {
       const int acc = t_local & 1;
@@ -449,18 +452,28 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3s(const ConvArgs a) {
       if (ok) {
         umma::fence_after_sync();
         const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * n3);
+        // P[r][1] and P[r][2] of 16 columns in flight together (one wait), to the exchange
 #pragma unroll
         for (int c0 = 0; c0 < co; c0 += 16) {
-          float t[16];
-          umma::tmem_ld16(trow + (uint32_t)c0, t);
+          uint32_t t1[16], t2[16];
+          umma::tmem_ld16_issue(trow + (uint32_t)(co + c0), t1);
+          umma::tmem_ld16_issue(trow + (uint32_t)(2 * co + c0), t2);
+          umma::tmem_wait_ld_tied(t1);
+          umma::tmem_tie(t2);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v0[c0 + j] = t[j];
-          umma::tmem_ld16(trow + (uint32_t)(co + c0), t);
+          for (int j = 0; j < 16; j += 4) {
+            *reinterpret_cast<uint4*>(x1 + r * xp + c0 + j) = make_uint4(t1[j], t1[j + 1], t1[j + 2], t1[j + 3]);
+            *reinterpret_cast<uint4*>(x2 + r * xp + c0 + j) = make_uint4(t2[j], t2[j + 1], t2[j + 2], t2[j + 3]);
+          }
+        }
+        // P[r][0], kept in registers across the exchange
 #pragma unroll
-          for (int j = 0; j < 16; ++j) x1[r * xp + c0 + j] = t[j];
-          umma::tmem_ld16(trow + (uint32_t)(2 * co + c0), t);
+        for (int c0 = 0; c0 < co; c0 += 16) {
+          uint32_t t0[16];
+          umma::tmem_ld16_issue(trow + (uint32_t)c0, t0);
+          umma::tmem_wait_ld_tied(t0);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) x2[r * xp + c0 + j] = t[j];
+          for (int j = 0; j < 16; ++j) v0[c0 + j] = __uint_as_float(t0[j]);
         }
         umma::fence_before_sync();
         umma::mbar_arrive(&acc_empty[acc]);  // TMEM read: the MMA warp may reuse it
@@ -478,11 +491,16 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3s(const ConvArgs a) {
         for (int c0 = 0; c0 < co; c0 += 16) {
           float v[16];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = v0[c0 + j] + x1[(r + 1) * xp + c0 + j] + x2[(r + 2) * xp + c0 + j];
-          if (a.bias) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] += __ldg(a.bias + c0 + j);
+          for (int j = 0; j < 16; j += 4) {
+            const float4 u1 = *reinterpret_cast<const float4*>(x1 + (r + 1) * xp + c0 + j);
+            const float4 u2 = *reinterpret_cast<const float4*>(x2 + (r + 2) * xp + c0 + j);
+            v[j] = v0[c0 + j] + u1.x + u2.x;
+            v[j + 1] = v0[c0 + j + 1] + u1.y + u2.y;
+            v[j + 2] = v0[c0 + j + 2] + u1.z + u2.z;
+            v[j + 3] = v0[c0 + j + 3] + u1.w + u2.w;
           }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] += bias_s[c0 + j];
           if (a.flags & PVD_UNET_ACT_LEAKY) {
 #pragma unroll
             for (int j = 0; j < 16; ++j) v[j] = v[j] > 0.f ? v[j] : v[j] * a.slope;
@@ -1041,8 +1059,8 @@ struct ConvPlanSm {
 };
 
 static size_t conv_smem_stacked(int cin, int cout, int na) {
-  return (size_t)na * (cin / 8) * STK_PITCH + (size_t)27 * cin * cout * 2 + (size_t)2 * STK_ROWS * (cout + 1) * 4 +
-         (size_t)(2 * na + 5) * 8 + 4 + 16;
+  return (size_t)na * (cin / 8) * STK_PITCH + (size_t)27 * cin * cout * 2 + (size_t)2 * STK_ROWS * (cout + 4) * 4 +
+         (size_t)(2 * na + 5) * 8 + 16 + (size_t)cout * 4 + 16;
 }
 
 static ConvPlanSm conv_plan(int cin, int cout) {
@@ -1473,6 +1491,79 @@ extern "C" pvd_status pvd_adam_step(float* params, const float* grads, float* m,
   k_adam<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(params, grads, m, v, n, lr, beta1, beta2, eps,
                                                               weight_decay, c1, c2);
   PVD_LAUNCH_CHECK("k_adam");
+  return PVD_OK;
+}
+
+namespace pvd {
+namespace {
+constexpr int kClipParts = 1024;
+
+// partial sums of squares of contiguous chunks, each a fixed-order tree sum
+__global__ void __launch_bounds__(256) k_sumsq_parts(const float* __restrict__ g, int64_t n, float* __restrict__ parts) {
+  __shared__ double red[256];
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+  double s = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s += (double)g[i] * (double)g[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) parts[blockIdx.x] = (float)red[0];
+}
+
+// norm = sqrt(sum of the parts); scale = min(1, max_norm / norm); 0 (the step's gradient
+// dropped) if the norm is not finite or, with spike_factor > 0, exceeds spike_factor times
+// the running mean of the accepted norms (work[kClipParts + 2]; skipped steps are counted
+// in work[kClipParts + 3])
+__global__ void __launch_bounds__(kClipParts) k_clip_scale(float* __restrict__ work, float max_norm,
+                                                           float spike_factor) {
+  __shared__ double red[kClipParts];
+  red[threadIdx.x] = (double)work[threadIdx.x];
+  __syncthreads();
+  for (int w = kClipParts / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double nrm = sqrt(red[0]);
+    const float mean = work[kClipParts + 2];
+    const bool spike = spike_factor > 0.f && mean > 0.f && nrm > (double)spike_factor * mean;
+    work[kClipParts] = (float)nrm;
+    if (!isfinite(nrm) || spike) {
+      work[kClipParts + 1] = 0.f;
+      work[kClipParts + 3] += 1.f;
+    } else {
+      work[kClipParts + 1] = (float)fmin(1.0, (double)max_norm / fmax(nrm, 1e-30));
+      work[kClipParts + 2] = mean > 0.f ? 0.98f * mean + 0.02f * (float)nrm : (float)nrm;
+    }
+  }
+}
+
+__global__ void k_clip_apply(float* __restrict__ g, int64_t n, const float* __restrict__ work) {
+  const float sc = work[kClipParts + 1];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    g[i] = (sc == 0.f) ? 0.f : g[i] * sc;  // a non-finite gradient is dropped, not propagated
+}
+}  // namespace
+}  // namespace pvd
+
+extern "C" pvd_status pvd_grad_clip(float* grads, int64_t n, float max_norm, float spike_factor, float* work,
+                                    pvd_stream stream) {
+  if (!grads || !work || n < 0) return set_error(PVD_ERR_ARG, "pvd_grad_clip: bad arguments");
+  if (!(max_norm > 0.f) || !std::isfinite(max_norm)) return set_error(PVD_ERR_ARG, "pvd_grad_clip: max_norm must be > 0");
+  if (!(spike_factor >= 0.f) || !std::isfinite(spike_factor))
+    return set_error(PVD_ERR_ARG, "pvd_grad_clip: spike_factor must be >= 0");
+  if (n == 0) return PVD_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  k_sumsq_parts<<<kClipParts, 256, 0, st>>>(grads, n, work);
+  PVD_LAUNCH_CHECK("k_sumsq_parts");
+  k_clip_scale<<<1, kClipParts, 0, st>>>(work, max_norm, spike_factor);
+  PVD_LAUNCH_CHECK("k_clip_scale");
+  k_clip_apply<<<blocks_for(n, 256), 256, 0, st>>>(grads, n, work);
+  PVD_LAUNCH_CHECK("k_clip_apply");
   return PVD_OK;
 }
 

@@ -121,14 +121,17 @@ def analytic_profile(symbol: str, voxel_size, shape=None) -> np.ndarray:
     return np.exp(-r / lam) / (r * r)
 
 
-def gy_per_bq_s_scale(symbol: str, voxel_size, water_density: float = 1.0) -> float:
+def gy_per_bq_s_scale(symbol: str, voxel_size, water_density: float = 1.0, energy_mev=None) -> float:
     """Mean beta energy per decay deposited in one voxel of water, in Gy per (Bq s):
-    E_mean [MeV] * 1.602176634e-13 [J/MeV] / (rho * dV [mm^3] * 1e-6 [kg / (g/cc mm^3)])."""
+    E_mean [MeV] * 1.602176634e-13 [J/MeV] / (rho * dV [mm^3] * 1e-6 [kg / (g/cc mm^3)]).
+    ``energy_mev`` replaces the nuclide's stated mean beta energy (e.g. the mean of the
+    spectrum the Monte Carlo samples, ``mc_physics.spectrum_mean``)."""
     v = _vox3(voxel_size)
     nuc = get_nuclide(symbol)
     if nuc.extra.get("alpha"):
         raise ValueError(f"{symbol} is an alpha emitter: no analytic beta profile; use kernel_profile='reference'")
-    return nuc.beta_mean_mev * JOULE_PER_MEV / (water_density * v[0] * v[1] * v[2] * 1e-6)
+    e = nuc.beta_mean_mev if energy_mev is None else float(energy_mev)
+    return e * JOULE_PER_MEV / (water_density * v[0] * v[1] * v[2] * 1e-6)
 
 
 def reference_profile(symbol: str, tissue: str, voxel_size: float, shape, fix_r0: bool = True) -> np.ndarray:

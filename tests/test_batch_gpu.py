@@ -180,3 +180,26 @@ def test_batch_fit_with_more_timepoints(times):
     assert np.median(rel[ok]) < 1e-6 and np.quantile(rel[ok], 0.99) < 1e-3
     assert torch.isfinite(d).all()
     bc.close()
+
+
+def test_autotuned_batch_stages_equal_the_graph(batch_case):
+    """With autotuned FFT lengths per volume shape the batch dose still matches the FP64
+    oracle convolution of the fit's cumulated activity at 1e-5, and the two directly
+    enqueued stages (every fit, then every convolution) reproduce the graph launch bit
+    for bit."""
+    from pyvoxeldosimetry_gb300.batch import BatchDoseCalculator
+    vols, truth = batch_case
+    bc = BatchDoseCalculator("Y90", use_graph=True, autotune=True)
+    dg = [x.clone() for x in bc.calculate(vols)]
+    torch.cuda.synchronize()
+    for i, ((auc, vs, rho), d) in enumerate(zip(truth, dg)):
+        cum = bc.cumulated(i).cpu().numpy().astype(np.float64)
+        ref = oc.density_scale(oc.linear_conv_same(cum, kernel_S("Y90", vs)), rho)
+        assert np.abs(d.cpu().numpy() - ref).max() / np.abs(ref).max() <= 1e-5
+    for d in bc.run():
+        d.zero_()                                   # the stages must write every voxel again
+    fit_ms, conv_ms = bc.run_stages()
+    assert fit_ms > 0 and conv_ms > 0
+    for i, d in enumerate(dg):
+        assert torch.equal(d, bc._items[i]["dose"][0])
+    bc.close()

@@ -26,7 +26,9 @@ def test_fallback_everywhere_returns_the_plain_convolution(setup):
     lc, net, path, act, rho = setup
     from pyvoxeldosimetry_gb300 import DoseCalculator, KernelConvolutionCalculator
     vox = (4.0, 4.0, 4.0)
-    plain = KernelConvolutionCalculator("Y90").calculate_dose_rate(act, vox, density=rho)
+    # the corrected calculator convolves at the energy per decay of the Monte Carlo it was trained against
+    plain = KernelConvolutionCalculator("Y90", config=lc.mc_consistent_config("Y90")).calculate_dose_rate(
+        act, vox, density=rho)
     calc = DoseCalculator("Y90", method="nn_corrected", config={"model_path": path, "sigma_max": 0.0})
     res = calc.calculate_dose(activity_maps=[act], voxel_size=vox, tissue_densities=rho)
     d = res.dose_rate_maps[0]
@@ -61,4 +63,5 @@ def test_without_density_the_plain_convolution_is_returned(setup):
     vox = (4.0, 4.0, 4.0)
     calc = NNCorrectedDoseCalculator("Y90", config={"model": net})
     assert np.array_equal(calc.calculate_dose_rate(act, vox),
-                          KernelConvolutionCalculator("Y90").calculate_dose_rate(act, vox))
+                          KernelConvolutionCalculator("Y90", config=lc.mc_consistent_config("Y90"))
+                          .calculate_dose_rate(act, vox))

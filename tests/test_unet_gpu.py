@@ -356,3 +356,33 @@ def test_adam_step(env):
         opt.step()
     # AdamW applies the decay as p *= (1 - lr wd) before the update; the kernel as lr wd p in the update
     assert _nrm(pd.cpu().double(), ref.detach()) <= 1e-5
+
+
+def test_gradient_clip_and_spike_skip():
+    """pvd_grad_clip: the global norm (FP64 partial sums) scales the gradients down to
+    max_norm; a non-finite norm, or one above spike_factor x the running mean of the
+    accepted norms, drops the step (gradients zeroed, counted in work[1027])."""
+    from pyvoxeldosimetry_gb300 import _native as N
+    lib = N.load()
+    dev = torch.device("cuda", 0)
+    g = torch.randn(100_003, generator=torch.Generator().manual_seed(1)).to(dev)
+    work = torch.zeros(1028, device=dev)
+    nrm = float(g.double().norm())
+    g1 = g.clone()
+    N.check(lib.pvd_grad_clip(g1.data_ptr(), g1.numel(), 1.0, 10.0, work.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert abs(float(work[1024]) - nrm) <= 1e-5 * nrm
+    assert torch.allclose(g1, g / nrm, rtol=1e-5, atol=1e-9) and abs(float(work[1026]) - nrm) <= 1e-5 * nrm
+    g2 = g.clone()                       # below max_norm: untouched
+    N.check(lib.pvd_grad_clip(g2.data_ptr(), g2.numel(), 2.0 * nrm, 10.0, work.data_ptr(), None))
+    assert torch.equal(g2, g)
+    g3 = g * 1000.0                      # a spike: dropped
+    N.check(lib.pvd_grad_clip(g3.data_ptr(), g3.numel(), 1.0, 10.0, work.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert float(g3.abs().max()) == 0.0 and float(work[1027]) == 1.0
+    g4 = g.clone()
+    g4[7] = float("nan")                 # non-finite: dropped, NaN not propagated
+    N.check(lib.pvd_grad_clip(g4.data_ptr(), g4.numel(), 1.0, 0.0, work.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert float(g4.abs().max()) == 0.0 and not torch.isnan(g4).any() and float(work[1027]) == 2.0
+    assert lib.pvd_grad_clip(g.data_ptr(), g.numel(), 0.0, 1.0, work.data_ptr(), None) == 1
