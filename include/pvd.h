@@ -643,13 +643,14 @@ pvd_status pvd_adam_step(float* params, const float* grads, float* m, float* v, 
 
 /* Global-norm gradient clipping before pvd_adam_step: norm = ||grads||_2 over n
  * FP32 values (fixed-order reduction, FP64 partial sums), then grads *= min(1,
- * max_norm / norm).  The gradients are zeroed (the step is then carried by
- * Adam's moments alone, which the outlier does not enter) when the norm is not
- * finite or, with spike_factor > 0, exceeds spike_factor times the running mean
- * of the norms accepted so far.  work: device float32 of PVD_GRAD_CLIP_WORK
- * values, zeroed before the first step and kept between steps: work[1024]
- * receives the norm, work[1025] the scale, work[1026] holds the running mean,
- * work[1027] counts the dropped steps.  No host round trip. */
+ * limit / norm), limit = max_norm or, with spike_factor > 0, the smaller of
+ * max_norm and spike_factor times the running mean of the limited norms (so one
+ * outlying crop cannot throw Adam's second moments off, while its gradient still
+ * acts).  A non-finite norm zeroes the gradients.  work: device float32 of
+ * PVD_GRAD_CLIP_WORK values, zeroed before the first step and kept between steps:
+ * work[1024] receives the norm, work[1025] the scale, work[1026] holds the
+ * running mean, work[1027] counts the steps the running-mean limit (or a
+ * non-finite norm) cut.  No host round trip. */
 #define PVD_GRAD_CLIP_WORK 1028
 pvd_status pvd_grad_clip(float* grads, int64_t n, float max_norm, float spike_factor, float* work,
                          pvd_stream stream);

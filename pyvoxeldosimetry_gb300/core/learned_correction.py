@@ -161,7 +161,7 @@ class TrainStats:
     loss_mu: List[float] = field(default_factory=list)
     loss_s: List[float] = field(default_factory=list)
     grad_norm: List[float] = field(default_factory=list)  # before clipping
-    skipped: int = 0                                      # steps dropped as gradient spikes
+    skipped: int = 0                                      # steps cut by the running-mean limit
 
 
 class UNet3D:
@@ -353,10 +353,10 @@ class UNet3D:
         self._wgrad("e0a", t["x0"], gr["e0a"], ws, stream)
 
     def clip_gradients(self, max_norm: float, spike_factor: float = 0.0, stream=None) -> None:
-        """Scale the parameter gradients to a global L2 norm of at most max_norm, and drop
-        them when the norm exceeds spike_factor times the running mean of earlier norms
+        """Scale the parameter gradients to a global L2 norm of at most max_norm and, with
+        spike_factor > 0, of at most spike_factor times the running mean of earlier norms
         (on the device; the norm before clipping is left in clip_work[1024], the count of
-        dropped steps in clip_work[1027])."""
+        steps the running-mean limit cut in clip_work[1027])."""
         N.check(self._lib.pvd_grad_clip(self.grads.data_ptr(), self.n_params, float(max_norm), float(spike_factor),
                                         self.clip_work.data_ptr(), _stream_handle(stream)))
 
@@ -486,10 +486,10 @@ def train(net: UNet3D, pairs: Sequence[TrainingPair], steps: int, crop=(32, 32, 
     """Adam on random crops of random pairs; a crop lies inside its volume when it
     fits, else covers it from a random offset.  The learning rate rises linearly over
     the first ``warmup`` fraction of the steps, then decays on a cosine; gradients are
-    clipped to a global norm of ``clip`` (0: no clipping), and a step whose gradient
-    norm exceeds ``spike_factor`` times the running mean of the earlier ones is dropped
-    before it reaches Adam's moments: one outlying crop would otherwise throw the
-    moments and the weights off course."""
+    clipped to a global norm of ``clip`` (0: no clipping) and to ``spike_factor`` times
+    the running mean of the earlier norms: one outlying crop would otherwise throw
+    Adam's second moments off course.  The direction of a clipped gradient is kept:
+    dropping such steps instead lets the momentum carry a diverging network further."""
     rng = np.random.default_rng(seed)
     ws = net.workspace(crop, train=True)
     stream = _stream_handle(None)

@@ -944,7 +944,6 @@ __device__ __forceinline__ void vp_store(const FitArgs& a, const VpVoxel<TM>& d,
   store_fit<M_F4A>(a, p, good, ymax, v, nvox, params, auc, ok, auc32);
 }
 
-// Marker in params[0] of a voxel that the FP64 polish left to the FP64 trust-region stage.
 constexpr int kVpPolished = 100;  // init code of a voxel the polish already stored
 
 // FP64 polish between the FP32 and the FP64 trust-region stages (PVD_FIT_MIXED): from

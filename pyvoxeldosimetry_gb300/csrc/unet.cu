@@ -139,9 +139,11 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
   uint64_t* acc_full = empty_b + nb;
   uint64_t* acc_empty = acc_full + 2;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(acc_empty + 2);
+  float* bias_s = reinterpret_cast<float*>(tslot + 4);  // [cout] bias (0 without one)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t ncols = umma::tmem_cols(2 * a.cout);
 
+  for (int i = threadIdx.x; i < a.cout; i += blockDim.x) bias_s[i] = a.bias ? __ldg(a.bias + i) : 0.f;
   if (threadIdx.x == 0) {
     for (int i = 0; i < na; ++i) {
       mbar_init(&full_a[i], 1);
@@ -271,14 +273,9 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
       const long long p = (long long)tile * TILE_M + r;
       const bool in = interior(g, p);
       const long long roff = (g.margin + p) * 16;
-      for (int c0 = 0; c0 < a.cout; c0 += 16) {
-        float v[16];
-        __syncwarp();
-        umma::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * a.cout + c0), v);
-        if (a.bias) {
+      auto finish16 = [&](int c0, float* v) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] += __ldg(a.bias + c0 + j);
-        }
+        for (int j = 0; j < 16; ++j) v[j] += bias_s[c0 + j];
         if (a.flags & PVD_UNET_ACT_LEAKY) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) v[j] = v[j] > 0.f ? v[j] : v[j] * a.slope;
@@ -304,6 +301,25 @@ __global__ void __launch_bounds__(CONV_THREADS, 1) k_conv3(const ConvArgs a) {
         }
         *reinterpret_cast<uint4*>(a.y + pl * a.plane + roff) = pack8(v);
         *reinterpret_cast<uint4*>(a.y + (pl + 1) * a.plane + roff) = pack8(v + 8);
+      };
+      const uint32_t trow = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * a.cout);
+      for (int c0 = 0; c0 < a.cout; c0 += 32) {  // two column groups of 16 in flight per wait
+        uint32_t t0[16], t1[16];
+        const bool two = c0 + 16 < a.cout;  // uniform: cout is a kernel argument
+        __syncwarp();
+        umma::tmem_ld16_issue(trow + (uint32_t)c0, t0);
+        if (two) umma::tmem_ld16_issue(trow + (uint32_t)(c0 + 16), t1);
+        umma::tmem_wait_ld_tied(t0);
+        umma::tmem_tie(t1);
+        float v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(t0[j]);
+        finish16(c0, v);
+        if (two) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(t1[j]);
+          finish16(c0 + 16, v);
+        }
       }
       umma::fence_before_sync();
       umma::mbar_arrive(&acc_empty[acc]);
@@ -1047,7 +1063,8 @@ static bool ch_ok(int c) { return c >= 16 && c <= 256 && c % 16 == 0; }
 static bool al16(const void* p) { return ((uintptr_t)p & 15) == 0; }
 
 static size_t conv_smem(int cin, int cout, int na, int nb) {
-  return (size_t)na * (cin / 8) * SLAB_PITCH + (size_t)nb * cin * cout * 2 + (size_t)(4 + 2 * na + 2 * nb) * 8 + 16;
+  return (size_t)na * (cin / 8) * SLAB_PITCH + (size_t)nb * cin * cout * 2 + (size_t)(4 + 2 * na + 2 * nb) * 8 + 16 +
+         (size_t)cout * 4 + 16;
 }
 
 // Shared-memory plan of a convolution: all 27 taps' weights resident with up to
@@ -1514,10 +1531,12 @@ __global__ void __launch_bounds__(256) k_sumsq_parts(const float* __restrict__ g
   if (threadIdx.x == 0) parts[blockIdx.x] = (float)red[0];
 }
 
-// norm = sqrt(sum of the parts); scale = min(1, max_norm / norm); 0 (the step's gradient
-// dropped) if the norm is not finite or, with spike_factor > 0, exceeds spike_factor times
-// the running mean of the accepted norms (work[kClipParts + 2]; skipped steps are counted
-// in work[kClipParts + 3])
+// norm = sqrt(sum of the parts); limit = max_norm, lowered to spike_factor times the
+// running mean of the (limited) norms when spike_factor > 0 (work[kClipParts + 2]);
+// scale = min(1, limit / norm), counted in work[kClipParts + 3] when the running-mean
+// limit bit; 0 (the step's gradient dropped) only for a non-finite norm.  A limited
+// gradient keeps its direction: dropping it instead lets Adam's momentum carry the
+// weights on, unopposed, when a rising loss makes every gradient look large.
 __global__ void __launch_bounds__(kClipParts) k_clip_scale(float* __restrict__ work, float max_norm,
                                                            float spike_factor) {
   __shared__ double red[kClipParts];
@@ -1530,14 +1549,18 @@ __global__ void __launch_bounds__(kClipParts) k_clip_scale(float* __restrict__ w
   if (threadIdx.x == 0) {
     const double nrm = sqrt(red[0]);
     const float mean = work[kClipParts + 2];
-    const bool spike = spike_factor > 0.f && mean > 0.f && nrm > (double)spike_factor * mean;
+    double limit = (double)max_norm;
+    const bool adaptive = spike_factor > 0.f && mean > 0.f && (double)spike_factor * mean < limit;
+    if (adaptive) limit = (double)spike_factor * mean;
     work[kClipParts] = (float)nrm;
-    if (!isfinite(nrm) || spike) {
+    if (!isfinite(nrm)) {
       work[kClipParts + 1] = 0.f;
       work[kClipParts + 3] += 1.f;
     } else {
-      work[kClipParts + 1] = (float)fmin(1.0, (double)max_norm / fmax(nrm, 1e-30));
-      work[kClipParts + 2] = mean > 0.f ? 0.98f * mean + 0.02f * (float)nrm : (float)nrm;
+      work[kClipParts + 1] = (float)fmin(1.0, limit / fmax(nrm, 1e-30));
+      if (adaptive && nrm > limit) work[kClipParts + 3] += 1.f;
+      const float used = (float)fmin(nrm, limit);
+      work[kClipParts + 2] = mean > 0.f ? 0.98f * mean + 0.02f * used : used;
     }
   }
 }

@@ -358,10 +358,10 @@ def test_adam_step(env):
     assert _nrm(pd.cpu().double(), ref.detach()) <= 1e-5
 
 
-def test_gradient_clip_and_spike_skip():
+def test_gradient_clip_and_running_mean_limit():
     """pvd_grad_clip: the global norm (FP64 partial sums) scales the gradients down to
-    max_norm; a non-finite norm, or one above spike_factor x the running mean of the
-    accepted norms, drops the step (gradients zeroed, counted in work[1027])."""
+    max_norm, and to spike_factor x the running mean of the earlier (limited) norms; a
+    non-finite norm zeroes them (counted in work[1027], like the limited steps)."""
     from pyvoxeldosimetry_gb300 import _native as N
     lib = N.load()
     dev = torch.device("cuda", 0)
@@ -372,16 +372,20 @@ def test_gradient_clip_and_spike_skip():
     N.check(lib.pvd_grad_clip(g1.data_ptr(), g1.numel(), 1.0, 10.0, work.data_ptr(), None))
     torch.cuda.synchronize()
     assert abs(float(work[1024]) - nrm) <= 1e-5 * nrm
-    assert torch.allclose(g1, g / nrm, rtol=1e-5, atol=1e-9) and abs(float(work[1026]) - nrm) <= 1e-5 * nrm
-    g2 = g.clone()                       # below max_norm: untouched
-    N.check(lib.pvd_grad_clip(g2.data_ptr(), g2.numel(), 2.0 * nrm, 10.0, work.data_ptr(), None))
-    assert torch.equal(g2, g)
-    g3 = g * 1000.0                      # a spike: dropped
-    N.check(lib.pvd_grad_clip(g3.data_ptr(), g3.numel(), 1.0, 10.0, work.data_ptr(), None))
+    assert torch.allclose(g1, g / nrm, rtol=1e-5, atol=1e-9)
+    assert abs(float(work[1026]) - 1.0) <= 1e-6          # running mean of the limited norms
+    g2 = g * (0.5 / nrm)                                  # below both limits: untouched
+    ref2 = g2.clone()
+    N.check(lib.pvd_grad_clip(g2.data_ptr(), g2.numel(), 100.0, 10.0, work.data_ptr(), None))
+    assert torch.equal(g2, ref2)
+    mean = float(work[1026])
+    g3 = g * (1000.0 / nrm)                               # a spike: cut to 10 x the running mean, direction kept
+    N.check(lib.pvd_grad_clip(g3.data_ptr(), g3.numel(), 1e6, 10.0, work.data_ptr(), None))
     torch.cuda.synchronize()
-    assert float(g3.abs().max()) == 0.0 and float(work[1027]) == 1.0
+    assert abs(float(g3.double().norm()) - 10.0 * mean) <= 1e-4 * 10.0 * mean and float(work[1027]) == 1.0
+    assert torch.allclose(g3 / g3.norm(), g / g.norm(), rtol=1e-4, atol=1e-7)
     g4 = g.clone()
-    g4[7] = float("nan")                 # non-finite: dropped, NaN not propagated
+    g4[7] = float("nan")                                  # non-finite: zeroed, NaN not propagated
     N.check(lib.pvd_grad_clip(g4.data_ptr(), g4.numel(), 1.0, 0.0, work.data_ptr(), None))
     torch.cuda.synchronize()
     assert float(g4.abs().max()) == 0.0 and not torch.isnan(g4).any() and float(work[1027]) == 2.0
