@@ -582,7 +582,9 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_inv(
             const int n = 32 * u + lane;
             if (n < N2) {
               float val = oc[rr * S + n];
-              if (dr) val = (d[u] > 0.f) ? val * __frcp_rn(d[u]) : 0.f;
+              // 2-ulp division (x * rcp.approx(d)): far inside the 1e-5 parity bound, and a
+              // fraction of the instructions of a correctly rounded one
+              if (dr) val = (d[u] > 0.f) ? __fdividef(val, d[u]) : 0.f;
               dst[n] = val;
             }
           }
