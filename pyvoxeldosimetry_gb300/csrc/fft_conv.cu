@@ -601,6 +601,47 @@ int persistent_grid(const void* fn, int threads, size_t smem, int dev) {
   return nb * sms;
 }
 
+// Lets f take the largest dynamic shared memory the device allows beside f's own static
+// shared memory; returns that allowance (0 when the attribute could not be set).
+size_t allow_dyn_smem(const void* f, int smem_max) {
+  cudaFuncAttributes a{};
+  if (cudaFuncGetAttributes(&a, f) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int allow = smem_max - (int)a.sharedSizeBytes;
+  if (allow <= 0 || cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, allow) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return (size_t)allow;
+}
+
+// Opts the pass kernels a plan launches (the register kernels of its fast lengths, else the
+// generic ones) into large tiles; false if a pass's tile does not fit beside its kernel's
+// static shared memory.  fl[i] serves axis i: x (rows) is axis 2, y axis 1, z axis 0.
+bool pass_tiles_fit(const FastLen* const fl[3], size_t smem_x, size_t smem_y, size_t smem_z, int smem_max) {
+  auto fits = [smem_max](const void* f, size_t need) { return need <= allow_dyn_smem(f, smem_max); };
+  bool ok = true;
+  if (fl[2]) {
+    ok = fits((const void*)fl[2]->x_fwd, fl[2]->smem_row) && ok;
+    ok = fits((const void*)fl[2]->x_inv, fl[2]->smem_row) && ok;
+  } else {
+    ok = fits((const void*)k_x_fwd, smem_x) && ok;
+    ok = fits((const void*)k_x_inv, smem_x) && ok;
+  }
+  if (fl[1]) {
+    ok = fits((const void*)fl[1]->y_fwd, fl[1]->smem_col) && ok;
+    ok = fits((const void*)fl[1]->y_inv, fl[1]->smem_col) && ok;
+  } else {
+    ok = fits((const void*)k_y<false>, smem_y) && ok;
+    ok = fits((const void*)k_y<true>, smem_y) && ok;
+  }
+  if (fl[0]) ok = fits((const void*)fl[0]->z, fl[0]->smem_z) && ok;
+  else ok = fits((const void*)k_z, smem_z) && ok;
+  return ok;
+}
+
 // Enables the TMA-staged y and z passes when both axes have register kernels;
 // leaves p->tma = 0 (plain register passes) if anything does not fit.
 pvd_status setup_tma(pvd_plan* p, int smem_max) {
@@ -616,14 +657,14 @@ pvd_status setup_tma(pvd_plan* p, int smem_max) {
   p->smem_tyf = tma_y_smem(fy->L, p->yf_chunks, p->yf_boxr);
   p->smem_tyi = tma_y_smem(fy->L, p->yi_chunks, p->yi_boxr);
   p->smem_tz = tma_z_smem(fz->L, p->z_chunks, p->z_boxr);
-  if ((int)std::max({p->smem_tyf, p->smem_tyi, p->smem_tz}) > smem_max) return PVD_OK;
+  if (p->smem_tyf > allow_dyn_smem((const void*)fy->ty_fwd, smem_max) ||
+      p->smem_tyi > allow_dyn_smem((const void*)fy->ty_inv, smem_max) ||
+      p->smem_tz > allow_dyn_smem((const void*)fz->tz, smem_max))
+    return PVD_OK;
   bool ok = encode_cols(&p->m_yf, p->buf1, p->HS, p->N[1], p->N[0], p->yf_boxr, 1) &&
             encode_cols(&p->m_z, p->buf2, p->HS, p->P[1], p->N[0], 1, p->z_boxr);
   for (int s = 0; s < p->nk && ok; ++s) ok = encode_cols(&p->m_yi[s], p->buf3[s], p->HS, p->P[1], p->N[0], p->yi_boxr, 1);
   if (!ok) return PVD_OK;
-  cudaFuncSetAttribute((const void*)fy->ty_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute((const void*)fy->ty_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute((const void*)fz->tz, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
   p->grid_yf = persistent_grid((const void*)fy->ty_fwd, fy->threads, p->smem_tyf, p->dev);
   p->grid_yi = persistent_grid((const void*)fy->ty_inv, fy->threads, p->smem_tyi, p->dev);
   p->grid_z = persistent_grid((const void*)fz->tz, fz->threads, p->smem_tz, p->dev);
@@ -698,26 +739,9 @@ extern "C" pvd_status pvd_plan_create(const pvd_conv_desc* d, pvd_plan** out) {
   p->smem_z = smem_bytes(p->P[0], p->nk > 1 ? 3 : 2);
   int smem_max = 0;
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->dev);
-  const size_t need_x = p->fl[2] ? p->fl[2]->smem_row : p->smem_x;
-  const size_t need_y = p->fl[1] ? p->fl[1]->smem_col : p->smem_y;
-  const size_t need_z = p->fl[0] ? p->fl[0]->smem_z : p->smem_z;
-  if ((int)std::max({need_x, need_y, need_z}) > smem_max) {
+  if (!pass_tiles_fit(p->fl, p->smem_x, p->smem_y, p->smem_z, smem_max)) {
     delete p;
     return set_error(PVD_ERR_UNSUPPORTED, "pvd_plan_create: FFT length too large for one shared-memory tile");
-  }
-  cudaFuncSetAttribute(k_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute(k_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute(k_y<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute(k_y<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute(k_z, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  for (int i = 0; i < 3; ++i) {
-    const FastLen* f = p->fl[i];
-    if (!f) continue;
-    cudaFuncSetAttribute((const void*)f->x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-    cudaFuncSetAttribute((const void*)f->x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-    cudaFuncSetAttribute((const void*)f->y_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-    cudaFuncSetAttribute((const void*)f->y_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-    cudaFuncSetAttribute((const void*)f->z, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
   }
 
   pvd_status st = PVD_OK;
@@ -1382,24 +1406,7 @@ extern "C" pvd_status pvd_conv_execute_static(const float* activity_d, const flo
   int smem_max = 0, cur = 0;
   PVD_CUDA_TRY(cudaGetDevice(&cur));
   PVD_CUDA_TRY(cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, cur));
-  cudaFuncSetAttribute(k_x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute(k_x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute(k_y<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute(k_y<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  cudaFuncSetAttribute(k_z, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  for (int i = 0; i < 3; ++i) {
-    const FastLen* f = p.fl[i];
-    if (!f) continue;
-    cudaFuncSetAttribute((const void*)f->x_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-    cudaFuncSetAttribute((const void*)f->x_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-    cudaFuncSetAttribute((const void*)f->y_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-    cudaFuncSetAttribute((const void*)f->y_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-    cudaFuncSetAttribute((const void*)f->z, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max);
-  }
-  const size_t need_x = p.fl[2] ? p.fl[2]->smem_row : p.smem_x;
-  const size_t need_y = p.fl[1] ? p.fl[1]->smem_col : p.smem_y;
-  const size_t need_z = p.fl[0] ? p.fl[0]->smem_z : p.smem_z;
-  if ((int)std::max({need_x, need_y, need_z}) > smem_max)
+  if (!pass_tiles_fit(p.fl, p.smem_x, p.smem_y, p.smem_z, smem_max))
     return set_error(PVD_ERR_UNSUPPORTED, "pvd_conv_execute_static: FFT length too large for one shared-memory tile");
 
   cudaStream_t st = (cudaStream_t)stream;

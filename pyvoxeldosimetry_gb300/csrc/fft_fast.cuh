@@ -508,7 +508,13 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_inv(
   const int S = N2 | 1;
   const long long row0 = (long long)blockIdx.x * ROWS;
   const int nr = (int)min((long long)ROWS, (long long)nrows - row0);
+  __shared__ long long roff[ROWS];  // element offset of each row of the tile in a slot's buffer
+  if (threadIdx.x < ROWS) {         // rows of a launch fit in 32 bits (n0 n1 <= 4096^2)
+    const int r = (int)row0 + threadIdx.x, z = r / N1;
+    roff[threadIdx.x] = ((long long)z * pitch + (r - z * N1)) * HS;
+  }
   load_tw<L>(tw, twg, NTH);
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = threadIdx.x % FTX, j = threadIdx.x / FTX;
   static_for<XINV_SLOTS>([&](auto is) {
@@ -518,8 +524,7 @@ __global__ void __launch_bounds__(FTX* cmax(A, B), x_min_blocks(A, B)) kf_x_inv(
       // every row of the tile in flight at once: asynchronous copies straight into shared memory
       if (warp < NWF) {
         for (int rr = warp; rr < nr; rr += NWF) {
-          const int r = (int)row0 + rr, z = r / N1;  // rows of a launch fit in 32 bits (n0 n1 <= 4096^2)
-          const float2* src = in + ((long long)z * pitch + (r - z * N1)) * HS;
+          const float2* src = in + roff[rr];
           float2* dsm = ((rr & 1) ? hb : ha) + (rr >> 1) * S2;
           constexpr int KU = (H + 31) / 32;
 #pragma unroll

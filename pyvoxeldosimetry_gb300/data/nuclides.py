@@ -86,11 +86,13 @@ def _vox3(voxel_size):
     return v
 
 
-def default_kernel_size(symbol: str, voxel_size) -> tuple:
+def default_kernel_size(symbol: str, voxel_size, density: float = 1.0) -> tuple:
     """Odd kernel dims covering +/- the nuclide's kernel reach (15 mm Y-90, 6 mm Lu-177,
-    7.5 mm I-131): 15^3 at 2 mm and 21^3 at 1.5 mm for Y-90, 9^3 / 11^3 at 1.5 mm."""
+    7.5 mm I-131) in a medium of the given density (reach / density): 15^3 at 2 mm and
+    21^3 at 1.5 mm for Y-90 in water, 9^3 / 11^3 at 1.5 mm."""
     nuc = get_nuclide(symbol)
-    return tuple(2 * int(math.floor(nuc.kernel_reach_mm / d + 1e-9)) + 1 for d in _vox3(voxel_size))
+    reach = nuc.kernel_reach_mm / float(density)
+    return tuple(2 * int(math.floor(reach / d + 1e-9)) + 1 for d in _vox3(voxel_size))
 
 
 def radius_grid(shape, voxel_size) -> np.ndarray:
@@ -112,12 +114,14 @@ def analytic_lambda_mm(symbol: str) -> float:
     return Y90_LAMBDA_MM * nuc.beta_csda_range_mm / NUCLIDES["Y90"].beta_csda_range_mm
 
 
-def analytic_profile(symbol: str, voxel_size, shape=None) -> np.ndarray:
-    """Un-normalised exp(-r/lambda)/r^2 kernel (FP64), centre voxel at r0."""
-    shape = tuple(shape) if shape is not None else default_kernel_size(symbol, voxel_size)
+def analytic_profile(symbol: str, voxel_size, shape=None, density: float = 1.0) -> np.ndarray:
+    """Un-normalised exp(-r/lambda)/r^2 kernel (FP64), centre voxel at r0.  ``density``
+    gives the kernel of a homogeneous medium of that density relative to water: the decay
+    length becomes lambda / density (ranges scale inversely with density)."""
+    shape = tuple(shape) if shape is not None else default_kernel_size(symbol, voxel_size, density)
     r = radius_grid(shape, voxel_size)
     r = np.where(r == 0.0, equal_volume_radius(voxel_size), r)
-    lam = analytic_lambda_mm(symbol)
+    lam = analytic_lambda_mm(symbol) / float(density)
     return np.exp(-r / lam) / (r * r)
 
 
