@@ -455,7 +455,7 @@ def measure_resample(device, shape=(256, 256, 256), reps=5):
             "workload": "resample_volume order 3, 256^3 float32, whole call"}
 
 
-def measure_unet(device, small=False, train_steps=20, reps=3):
+def measure_unet(device, small=False, train_steps=1000, reps=3):
     """Learned correction: one training step (forward, both gradients, Adam) on a
     64^3 crop, NN-corrected dose (plain density-scaled convolution + U-Net +
     apply) of a 128^3 CT-like phantom at 3 mm, and the GPU Monte Carlo run to 1 %
@@ -499,25 +499,23 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
         e1.record()
         e1.synchronize()
         inf_ms.append(e0.elapsed_time(e1))
-    conv_t, inf_t = float(np.median(conv_ms)), float(np.median(inf_ms))
+    # the calculator's default: the prediction averaged over the 8 grid flips
+    lc.predict(net, a, r, dc, out=out, symmetries=8)
+    inf8_ms = []
+    for _ in range(reps):
+        e0.record()
+        lc.predict(net, a, r, dc, out=out, symmetries=8)
+        e1.record()
+        e1.synchronize()
+        inf8_ms.append(e0.elapsed_time(e1))
+    conv_t, inf_t, inf8_t = float(np.median(conv_ms)), float(np.median(inf_ms)), float(np.median(inf8_ms))
+    # whole training steps through the library's loop (focused crop, forward, loss, both
+    # gradients, clipping, Adam), host clock around the loop with a device sync at its end:
+    # forward and layer backward replayed as CUDA graphs (the default), and eager
     lc.train(net, [pair], 3, crop=crop)
-    s = torch.cuda.current_stream().cuda_stream
-    ws = net.workspace(crop, train=True)
-
-    def one_step():
-        net.pack_input(ws, (pair.activity, pair.density, pair.dose_conv), pair.scales, (0, 0, 0), s)
-        net.forward(ws, s)
-        net.backward(ws, pair.target, pair.weight, (0, 0, 0), s)
-        net.adam(lr=1e-4)
-
-    one_step()
-    torch.cuda.synchronize()
-    e0.record()
-    for _ in range(train_steps):
-        one_step()
-    e1.record()
-    e1.synchronize()
-    step_ms = e0.elapsed_time(e1) / train_steps
+    step_ms = lc.train(net, [pair], train_steps, crop=crop, lr=1e-4).seconds / train_steps * 1e3
+    eager_ms = lc.train(net, [pair], train_steps // 4, crop=crop, lr=1e-4, graphs=False).seconds / (
+        train_steps // 4) * 1e3
     # forward + data gradient (all but the first layer) + weight gradient
     fwd = lc.conv_flops(crop)
     first = 2.0 * 27 * 16 * 16 * crop[0] * crop[1] * crop[2]
@@ -545,15 +543,18 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
     rse = st.std(0, ddof=1)[sel] / np.sqrt(10) / mean[sel]
     rse_med = float(np.median(rse))
     mc_1pct_ms = mc_ms * (rse_med / 0.01) ** 2
-    nn_ms = conv_t + inf_t
+    nn_ms = conv_t + inf8_t
     return {
         "value": nvox / (nn_ms / 1e3) / 1e9, "unit": "Gvoxel/s (NN-corrected dose)",
         "workload": f"Y-90, {list(shape)} CT-like phantom at 3 mm: density-scaled conv + U-Net "
-                    f"(4 levels, 16-128 ch) + apply; training step on a {list(crop)} crop",
-        "plain_conv_ms": conv_t, "unet_inference_ms": inf_t, "nn_corrected_ms": nn_ms,
+                    f"(4 levels, 16-128 ch) averaged over the 8 grid flips + apply; training step on a "
+                    f"{list(crop)} crop",
+        "plain_conv_ms": conv_t, "unet_inference_ms": inf_t, "unet_inference_8_flips_ms": inf8_t,
+        "nn_corrected_ms": nn_ms, "nn_corrected_single_pass_ms": conv_t + inf_t,
         "plain_conv_gvox_s": nvox / (conv_t / 1e3) / 1e9,
         "unet_inference_tflops": lc.conv_flops(infer_crop) / (inf_t / 1e3) / 1e12,
-        "train_step_ms": step_ms, "train_step_tflops": step_flops / (step_ms / 1e3) / 1e12,
+        "train_step_ms": step_ms, "train_step_eager_ms": eager_ms,
+        "train_step_tflops": step_flops / (step_ms / 1e3) / 1e12,
         "train_tensor_frac": step_flops / (step_ms / 1e3) / 1e12 / tc_peak,
         "tensor_peak_tflops": tc_peak, "tensor_peak_source": tc_src,
         "mc_histories_per_batch": hb, "mc_ms_10_batches": mc_ms, "mc_median_rel_se": rse_med,
@@ -566,8 +567,9 @@ def measure_unet(device, small=False, train_steps=20, reps=3):
 
 def measure_unet_large(device, net, reps=2):
     """NN-corrected dose of one whole-body 512x512x400 volume at 1.5 mm (the whole-body
-    inference size): plain density-scaled Y-90 convolution + U-Net + apply, CUDA events
-    around each call, inputs resident."""
+    inference size): plain density-scaled Y-90 convolution + U-Net (single pass, and
+    averaged over the 8 grid flips) + apply, CUDA events around each call, inputs
+    resident."""
     import torch
     from pyvoxeldosimetry_gb300 import phantoms
     from pyvoxeldosimetry_gb300.core import learned_correction as lc
@@ -594,13 +596,19 @@ def measure_unet_large(device, net, reps=2):
         e1.record()
         e1.synchronize()
         inf_ms.append(e0.elapsed_time(e1))
+    e0.record()
+    lc.predict(net, a, r, d, out=out, symmetries=8)
+    e1.record()
+    e1.synchronize()
+    inf8 = e0.elapsed_time(e1)
     net.status()
     kshape = conv._kernel_specs(vox)[0][0].shape
     conv.close()
     c, i = float(np.median(conv_ms)), float(np.median(inf_ms))
     nvox = float(np.prod(shape))
     res = {"shape": list(shape), "plain_conv_ms": c, "unet_inference_ms": i, "nn_corrected_ms": c + i,
-           "nn_corrected_gvox_s": nvox / ((c + i) / 1e3) / 1e9,
+           "nn_corrected_gvox_s": nvox / ((c + i) / 1e3) / 1e9, "unet_inference_8_flips_ms": inf8,
+           "nn_corrected_8_flips_ms": c + inf8,
            "unet_inference_tflops": lc.conv_flops(shape) / (i / 1e3) / 1e12,
            "device_memory_peak_gb": torch.cuda.max_memory_allocated(device) / 1e9}
     # plain convolution against the FP64 oracle on a slab of 16 z planes through the middle:
@@ -622,14 +630,20 @@ def measure_unet_large(device, net, reps=2):
     return res
 
 
-def measure_unet_accuracy(device, small=False, n_train=128, steps=20000, nuclides=("Y90", "Lu177")):
+UNET_ACCURACY_STEPS = {"Y90": 120000, "Lu177": 40000}
+
+
+def measure_unet_accuracy(device, small=False, n_train=128, steps=None, nuclides=("Y90", "Lu177")):
     """What the learned correction gains, measured in the same run, per nuclide: the U-Net
     trained on this package's own pairs (seeded 128^3 CT-like phantoms at 3 mm — the kind
     the MC-to-1 % time is measured on — density-scaled convolution at the Monte Carlo's
     energy per decay vs GPU Monte Carlo with 1e8 histories; Y-90 betas, Lu-177 betas and
-    gammas), judged on 10 held-out phantoms against Monte Carlo with 4e8 histories (about
-    0.4 % statistical uncertainty in the judged voxels), tissue voxels above 10 % of the
-    tissue maximum: relative error of the plain and of the corrected dose."""
+    gammas; crops centred on weighted voxels; UNET_ACCURACY_STEPS Adam steps unless
+    ``steps`` says otherwise), judged on 10 held-out phantoms against Monte Carlo with
+    4e8 histories (about 0.4 % statistical uncertainty in the judged voxels), tissue
+    voxels above 10 % of the tissue maximum: relative error of the plain dose, of the
+    corrected dose averaged over the 8 grid flips (the calculator's default) and of the
+    single-pass corrected dose."""
     from pyvoxeldosimetry_gb300.core import learned_correction as lc
     shape, vox = ((48, 48, 48), 4.0) if small else ((128, 128, 128), 3.0)
     n_held, hist_held = (2, 200_000_000) if small else (10, 400_000_000)
@@ -640,18 +654,21 @@ def measure_unet_accuracy(device, small=False, n_train=128, steps=20000, nuclide
     out = {}
     for nuc in nuclides:
         t0 = time.perf_counter()
+        n_steps = steps or UNET_ACCURACY_STEPS.get(nuc, 40000)
         pairs = lc.generate_training_pairs(n_train, shape, vox, nuc, histories=hist, seed=100, device=device)
         held = lc.generate_training_pairs(n_held, shape, vox, nuc, histories=hist_held, seed=900, device=device)
         net = lc.UNet3D(seed=0, device=device)
-        st = lc.train(net, pairs, steps, crop=crop, lr=5e-4)
-        res = {"plain": [], "corrected": []}
+        st = lc.train(net, pairs, n_steps, crop=crop, lr=5e-4)
+        res = {"plain": [], "corrected": [], "corrected_single_pass": []}
         for p in held:
-            corr = lc.predict(net, p.activity, p.density, p.dose_conv, sigma_max=float("inf"))
+            corr = lc.predict(net, p.activity, p.density, p.dose_conv, sigma_max=float("inf"), symmetries=8)
+            single = lc.predict(net, p.activity, p.density, p.dose_conv, sigma_max=float("inf"))
             mc, rho = p.dose_mc.cpu().numpy(), p.density.cpu().numpy()
             res["plain"].append(lc.dose_errors(p.dose_conv.cpu().numpy(), mc, density=rho))
             res["corrected"].append(lc.dose_errors(corr.cpu().numpy(), mc, density=rho))
+            res["corrected_single_pass"].append(lc.dose_errors(single.cpu().numpy(), mc, density=rho))
         net.status()
-        # the judge's own noise: a second, independent Monte Carlo of the first held-out
+        # the reference Monte Carlo's own noise: a second, independent run on the first held-out
         # phantoms against the first (their difference carries sqrt(2) x one run's noise;
         # within 3 sqrt(2) % is where an exact prediction would land within 3 % of one run)
         from pyvoxeldosimetry_gb300.core.monte_carlo import MonteCarloCalculator
@@ -669,9 +686,10 @@ def measure_unet_accuracy(device, small=False, n_train=128, steps=20000, nuclide
         mc2.close()
         agg = {k: {m: float(np.mean([e[m] for e in v])) for m in ("mean", "median", "p95", "within_3pct")}
                for k, v in res.items()}
-        out[nuc] = {"train_steps": steps, "train_phantoms": n_train, "train_seconds": st.seconds,
+        out[nuc] = {"train_steps": n_steps, "train_phantoms": n_train, "train_seconds": st.seconds,
                     "skipped_steps": st.skipped, "total_seconds": time.perf_counter() - t0,
                     "held_out_phantoms": len(held), "plain_vs_mc": agg["plain"], "corrected_vs_mc": agg["corrected"],
+                    "corrected_single_pass_vs_mc": agg["corrected_single_pass"], "symmetries": 8,
                     "worst_phantom_within_3pct": float(min(e["within_3pct"] for e in res["corrected"])),
                     "mc_vs_mc_within_3pct": float(np.mean([f[0] for f in floor])),
                     "exact_prediction_within_3pct_estimate": float(np.mean([f[1] for f in floor])),

@@ -584,6 +584,35 @@ pvd_status pvd_unet_pack_input(const pvd_unet_geom* geom, const float* const* vo
                                const float* scales_d, const int* modes, int n_in, const int* vol_dims,
                                const int* origin, void* x, pvd_stream stream);
 
+/* Symmetries of the voxel grid, for averaging the network's prediction over them
+ * (the dose physics is invariant under flips, and under axis permutations of a grid
+ * with equal voxel sizes along the permuted axes).  Code s in [0, 48): the axis
+ * permutation s / 8 -- 0 (0,1,2), 1 (0,2,1), 2 (1,0,2), 3 (1,2,0), 4 (2,0,1),
+ * 5 (2,1,0), C-order axes -- followed by flips of the permuted axes in the bits of
+ * s % 8 (bit k: axis k).  The transformed volume is U = flip(transpose(V, perm),
+ * flipped axes) in numpy's meaning, of dims vol_dims[perm[k]].  Codes 0..7 are the
+ * flips alone. */
+#define PVD_UNET_SYMMETRIES 48
+
+/* pvd_unet_pack_input of the transformed volumes U (vol_dims: the dims of V, the
+ * untransformed volumes; origin in U's coordinates; geom: a crop of U).  sym 0 is
+ * pvd_unet_pack_input itself. */
+pvd_status pvd_unet_pack_input_sym(const pvd_unet_geom* geom, const float* const* volumes, const float* scales,
+                                   const float* scales_d, const int* modes, int n_in, const int* vol_dims,
+                                   const int* origin, int sym, void* x, pvd_stream stream);
+
+/* Average of predictions over symmetries, in the untransformed frame: for every
+ * voxel v of V (vol_dims) and both channels c (mu, s),
+ *   pred_avg[c][v] = (accumulate ? pred_avg[c][v] : 0) + weight * pred_sym[c][T(v)]
+ * where T maps v to U's coordinates for `sym`.  pred_sym: [2][geom_sym dims], a
+ * whole-volume prediction of U at origin 0 (pvd_unet_head on a crop of U, dims
+ * >= U's); pred_avg: [2][geom dims] (dims >= V's), the layout
+ * pvd_unet_apply_correction reads at origin 0.  Crop voxels outside V are not
+ * written. */
+pvd_status pvd_unet_symmetry_accumulate(const pvd_unet_geom* geom_sym, const float* pred_sym,
+                                        const pvd_unet_geom* geom, const int* vol_dims, int sym, float weight,
+                                        int accumulate, float* pred_avg, pvd_stream stream);
+
 /* 2x2x2 average pooling (fine dims = 2 x coarse dims) and its backward:
  * dx = ((accumulate ? dx : 0) + dy[parent] / 8) * (mask ? leaky'(mask) : 1). */
 pvd_status pvd_unet_pool(const pvd_unet_geom* fine, const void* x, const pvd_unet_geom* coarse, void* y, int channels,

@@ -47,7 +47,8 @@ EXPORTED_SYMBOLS = [
     "pvd_hu_composition",
     "pvd_radial_kernel",
     "pvd_unet_geometry", "pvd_unet_conv3d", "pvd_unet_wgrad_workspace", "pvd_unet_conv3d_wgrad",
-    "pvd_unet_pack_weights", "pvd_unet_pack_input", "pvd_unet_pool", "pvd_unet_pool_backward",
+    "pvd_unet_pack_weights", "pvd_unet_pack_input", "pvd_unet_pack_input_sym", "pvd_unet_symmetry_accumulate",
+    "pvd_unet_pool", "pvd_unet_pool_backward",
     "pvd_unet_upsample", "pvd_unet_upsample_backward", "pvd_unet_head", "pvd_unet_head_loss_workspace",
     "pvd_unet_head_loss", "pvd_unet_apply_correction", "pvd_unet_input_maxima", "pvd_unet_bias_grad_workspace", "pvd_unet_bias_grad", "pvd_adam_step", "pvd_grad_clip",
     "pvd_unet_status",
@@ -56,6 +57,7 @@ EXPORTED_SYMBOLS = [
 ]
 PVD_WAITCHECK_PLAN, PVD_WAITCHECK_UNET = 0, 1
 PVD_HU_ARTIFACTS = 1
+PVD_UNET_SYMMETRIES = 48
 
 
 class PvdError(RuntimeError):
@@ -183,6 +185,10 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_unet_pack_weights": (st, [vp, i, i, vp, vp, vp]),
         "pvd_unet_pack_input": (st, [C.POINTER(UnetGeom), C.POINTER(vp), C.POINTER(f), vp, C.POINTER(i), i,
                                      C.POINTER(i), C.POINTER(i), vp, vp]),
+        "pvd_unet_pack_input_sym": (st, [C.POINTER(UnetGeom), C.POINTER(vp), C.POINTER(f), vp, C.POINTER(i), i,
+                                         C.POINTER(i), C.POINTER(i), i, vp, vp]),
+        "pvd_unet_symmetry_accumulate": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), C.POINTER(i), i, f, i,
+                                              vp, vp]),
         "pvd_unet_pool": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), vp, i, vp]),
         "pvd_unet_pool_backward": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), vp, vp, i, i, f, vp]),
         "pvd_unet_upsample": (st, [C.POINTER(UnetGeom), vp, C.POINTER(UnetGeom), vp, i, vp]),

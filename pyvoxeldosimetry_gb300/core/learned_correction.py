@@ -29,6 +29,7 @@ are covered by crops that may overhang the volume (zero input there).
 from __future__ import annotations
 
 import ctypes as C
+import itertools
 import math
 import time
 from dataclasses import dataclass, field
@@ -195,6 +196,7 @@ class UNet3D:
         self.clip_work = torch.zeros(1028, dtype=torch.float32, device=self.device)
         self.step = 0
         self._ws: Dict[Tuple[Tuple[int, int, int], bool], _Workspace] = {}
+        self._sym: Dict[Tuple[int, int, int], torch.Tensor] = {}
         self._packed_for = -1
 
     # --- parameters -------------------------------------------------------
@@ -224,6 +226,13 @@ class UNet3D:
                                                     self._ptr(self.packed_fwd, po), self._ptr(self.packed_bwd, po),
                                                     stream))
         self._packed_for = self.step
+
+    def _sym_buffer(self, crop) -> torch.Tensor:
+        """[2 * crop voxels] FP32: the symmetry-averaged prediction (mu then s) of a crop."""
+        buf = self._sym.get(crop)
+        if buf is None:
+            buf = self._sym[crop] = torch.empty(2 * int(np.prod(crop)), dtype=torch.float32, device=self.device)
+        return buf
 
     def workspace(self, dims, train: bool) -> _Workspace:
         key = (tuple(int(d) for d in dims), bool(train))
@@ -261,8 +270,10 @@ class UNet3D:
         N.check(self._lib.pvd_unet_upsample(C.byref(x.geom), x.ptr, C.byref(y.geom), y.ptr, x.channels, stream))
 
     # --- passes -----------------------------------------------------------
-    def pack_input(self, ws: _Workspace, volumes: Sequence[torch.Tensor], scales, origin, stream) -> None:
-        """scales: host floats, or a device float32 tensor of len(volumes) scales."""
+    def pack_input(self, ws: _Workspace, volumes: Sequence[torch.Tensor], scales, origin, stream, sym: int = 0) -> None:
+        """scales: host floats, or a device float32 tensor of len(volumes) scales.  ``sym``
+        packs the volumes transformed by that grid symmetry (``symmetry``); origin and the
+        workspace's crop are then in the transformed frame."""
         vd = volumes[0].shape
         n = len(volumes)
         vp = (C.c_void_p * n)(*[v.data_ptr() for v in volumes])
@@ -273,8 +284,8 @@ class UNet3D:
         md = (C.c_int * n)(*INPUT_MODES[:n])
         dims = (C.c_int * 3)(*[int(d) for d in vd])
         org = (C.c_int * 3)(*[int(o) for o in origin])
-        N.check(self._lib.pvd_unet_pack_input(C.byref(ws.geo[0]), vp, sc, sc_d, md, n, dims, org, ws.t["x0"].ptr,
-                                              stream))
+        N.check(self._lib.pvd_unet_pack_input_sym(C.byref(ws.geo[0]), vp, sc, sc_d, md, n, dims, org, int(sym),
+                                                  ws.t["x0"].ptr, stream))
 
     def forward(self, ws: _Workspace, stream) -> torch.Tensor:
         """Run the network on ws.t['x0']; returns pred [2 * D*H*W] (mu then s)."""
@@ -307,6 +318,11 @@ class UNet3D:
     def backward(self, ws: _Workspace, target: torch.Tensor, weight: torch.Tensor, origin, stream) -> None:
         """Loss on the crop at `origin` of the target / weight volumes, and every
         parameter gradient into self.grads (the two loss values after them)."""
+        self.head_loss(ws, target, weight, origin, stream)
+        self.backward_layers(ws, stream)
+
+    def head_loss(self, ws: _Workspace, target: torch.Tensor, weight: torch.Tensor, origin, stream) -> None:
+        """The loss, the head's gradients and the gradient into the last layer."""
         if not ws.gr:
             raise RuntimeError("workspace was created for inference only")
         t, gr, lib = ws.t, ws.gr, self._lib
@@ -316,6 +332,13 @@ class UNet3D:
                                        ws.pred.data_ptr(), target.data_ptr(), weight.data_ptr(), vd, org, EPS, SLOPE,
                                        gr["d0b"].ptr, self._ptr(self.grads, self.head_offset),
                                        ws.scratch.data_ptr(), ws.scratch.numel(), stream))
+
+    def backward_layers(self, ws: _Workspace, stream) -> None:
+        """Every layer's parameter gradients, from the gradient head_loss left in the
+        last layer (no per-crop arguments: the same launches every step)."""
+        if not ws.gr:
+            raise RuntimeError("workspace was created for inference only")
+        t, gr, lib = ws.t, ws.gr, self._lib
         g0, g1, g2, g3 = (C.byref(x) for x in ws.geo)
         self._wgrad("d0b", t["d0a"], gr["d0b"], ws, stream)
         self._dgrad("d0b", gr["d0b"], gr["d0a"], t["d0a"], stream)
@@ -414,15 +437,22 @@ def log_ratio_target(dose_conv: np.ndarray, dose_mc: np.ndarray, density: np.nda
                      rel_threshold: float = 0.1) -> Tuple[np.ndarray, np.ndarray, float]:
     """Training target and weight of one phantom (host arithmetic: data preparation,
     not the dose path).  Weighted voxels: tissue (density >= TISSUE_DENSITY) whose
-    convolution dose exceeds rel_threshold x its maximum over tissue, with both doses
-    positive; target log(D_MC / D_conv) clipped to [-3, 3] there, 0 elsewhere.  Air is
-    excluded because dose to local mass there is dominated by the 1000x smaller mass,
-    in both methods.  Returns (target float32, weight float32, tissue dose maximum)."""
+    convolution dose exceeds rel_threshold x its maximum over tissue, or whose Monte
+    Carlo dose exceeds rel_threshold x the Monte Carlo's maximum over tissue, with both
+    doses positive; target log(D_MC / D_conv) clipped to [-3, 3] there, 0 elsewhere.
+    The Monte Carlo test matters in lung: a beta's range there is about three times its
+    range in water, the Monte Carlo dose reaches ten times the convolution's, and a
+    selection on the convolution dose alone leaves about a third of the lung voxels
+    above 10 % of the Monte Carlo maximum out of the loss (Y-90, 3 mm phantoms).  Air
+    is excluded because dose to local mass there is dominated by the 1000x smaller
+    mass, in both methods.  Returns (target float32, weight float32, tissue maximum of
+    the convolution dose)."""
     dc = np.asarray(dose_conv, np.float64)
     dm = np.asarray(dose_mc, np.float64)
     tissue = np.asarray(density) >= TISSUE_DENSITY
     dmax = float(dc[tissue].max()) if tissue.any() else float(dc.max())
-    ok = tissue & (dc > rel_threshold * dmax) & (dm > 0) & (dc > 0)
+    mmax = float(dm[tissue].max()) if tissue.any() else float(dm.max())
+    ok = tissue & ((dc > rel_threshold * dmax) | (dm > rel_threshold * mmax)) & (dm > 0) & (dc > 0)
     tgt = np.zeros(dc.shape, np.float32)
     tgt[ok] = np.clip(np.log(dm[ok] / dc[ok]), -3.0, 3.0)
     return tgt, ok.astype(np.float32), dmax
@@ -480,34 +510,70 @@ def generate_training_pairs(n: int, shape=(64, 64, 64), voxel_mm: float = 4.0, r
     return pairs
 
 
+def crop_origin(rng: np.random.Generator, vd, crop, hot: Optional[np.ndarray] = None) -> List[int]:
+    """Origin of a training crop of a volume of dims vd: inside the volume where the
+    crop fits, else covering it (origin in [vd - crop, 0]).  With ``hot`` (flat indices
+    of weighted voxels) the crop holds one of them, drawn uniformly, at a uniformly
+    random place within the crop, clamped to the same range (which keeps it inside)."""
+    lo = [min(0, vd[k] - c) for k, c in enumerate(crop)]
+    hi = [max(0, vd[k] - c) for k, c in enumerate(crop)]
+    if hot is not None and hot.size:
+        v = np.unravel_index(int(hot[int(rng.integers(hot.size))]), vd)
+        return [min(max(int(v[k]) - int(rng.integers(c)), lo[k]), hi[k]) for k, c in enumerate(crop)]
+    return [int(rng.integers(lo[k], hi[k] + 1)) for k in range(3)]
+
+
 def train(net: UNet3D, pairs: Sequence[TrainingPair], steps: int, crop=(32, 32, 32), lr: float = 2e-3,
           seed: int = 0, log_every: int = 0, clip: float = 1.0, warmup: float = 0.05,
-          spike_factor: float = 10.0) -> TrainStats:
+          spike_factor: float = 10.0, focus: bool = True, graphs: bool = True) -> TrainStats:
     """Adam on random crops of random pairs; a crop lies inside its volume when it
-    fits, else covers it from a random offset.  The learning rate rises linearly over
+    fits, else covers it from a random offset.  With ``focus`` every crop holds a
+    weighted voxel drawn uniformly from the pair's weighted voxels, at a uniformly
+    random place in the crop: the loss lives on a few tenths of a percent of the
+    voxels (tissue near the activity), and a crop without any gives a zero gradient
+    that Adam's momentum still steps on.  The learning rate rises linearly over
     the first ``warmup`` fraction of the steps, then decays on a cosine; gradients are
     clipped to a global norm of ``clip`` (0: no clipping) and to ``spike_factor`` times
     the running mean of the earlier norms: one outlying crop would otherwise throw
     Adam's second moments off course.  The direction of a clipped gradient is kept:
-    dropping such steps instead lets the momentum carry a diverging network further."""
+    dropping such steps instead lets the momentum carry a diverging network further.
+    With ``graphs`` the launches that take no per-crop argument -- weight packing and
+    the forward pass; every layer's backward -- are recorded once as two CUDA graphs
+    and replayed, leaving four library calls per step on the host (input packing,
+    loss head, clipping, Adam) instead of about ninety."""
     rng = np.random.default_rng(seed)
     ws = net.workspace(crop, train=True)
     stream = _stream_handle(None)
     stats = TrainStats()
+    hot = [np.flatnonzero(p.weight.cpu().numpy().ravel()) if focus else None for p in pairs]
     torch.cuda.synchronize(net.device)
     t0 = time.perf_counter()
+    g_fwd = g_bwd = None
     for it in range(steps):
-        p = pairs[int(rng.integers(len(pairs)))]
-        vd = p.activity.shape
-        origin = [int(rng.integers(min(0, vd[k] - c), max(0, vd[k] - c) + 1)) for k, c in enumerate(crop)]
+        ip = int(rng.integers(len(pairs)))
+        p = pairs[ip]
+        origin = crop_origin(rng, tuple(p.activity.shape), crop, hot[ip])
         net.pack_input(ws, (p.activity, p.density, p.dose_conv), p.scales, origin, stream)
-        net.forward(ws, stream)
-        net.backward(ws, p.target, p.weight, origin, stream)
+        if g_fwd is not None:
+            g_fwd.replay()
+            net.head_loss(ws, p.target, p.weight, origin, stream)
+            g_bwd.replay()
+        else:
+            net.forward(ws, stream)
+            net.backward(ws, p.target, p.weight, origin, stream)
         nw = max(1, int(warmup * steps))
         lr_t = lr * (it + 1) / nw if it < nw else lr * 0.5 * (1 + math.cos(math.pi * (it - nw) / max(1, steps - nw)))
         if clip > 0:
             net.clip_gradients(clip, spike_factor if it >= nw else 0.0)
         net.adam(lr=lr_t)
+        if graphs and it == 0 and steps > 1:
+            # recorded after one eager step (every launch configuration is set up by then)
+            g_fwd, g_bwd = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+            net._packed_for = -1
+            with torch.cuda.graph(g_fwd):
+                net.forward(ws, _stream_handle(None))
+            with torch.cuda.graph(g_bwd):
+                net.backward_layers(ws, _stream_handle(None))
         if log_every and (it % log_every == 0 or it == steps - 1):
             lm, ls = net.losses()
             stats.loss_mu.append(lm)
@@ -515,20 +581,45 @@ def train(net: UNet3D, pairs: Sequence[TrainingPair], steps: int, crop=(32, 32, 
             stats.grad_norm.append(float(net.clip_work[1024]))
     torch.cuda.synchronize(net.device)
     stats.seconds = time.perf_counter() - t0
+    net._packed_for = -1  # the graph's packing does not track the step count
     stats.steps = steps
     stats.skipped = net.skipped_steps()
     net.status()
     return stats
 
 
+SYMMETRY_SETS = (1, 8, 48)  # identity; the 8 flips; flips and the 6 axis permutations
+
+
+def symmetry(code: int) -> Tuple[Tuple[int, int, int], Tuple[int, ...]]:
+    """(axis permutation, flipped axes) of grid symmetry ``code`` in [0, 48), as the
+    library numbers them: permutation code // 8 of (0, 1, 2) in lexicographic order,
+    then the axes k of the permuted volume with bit k of code % 8 set flipped.  The
+    transformed volume is ``np.flip(np.transpose(v, perm), flips)``."""
+    if not 0 <= code < N.PVD_UNET_SYMMETRIES:
+        raise ValueError("symmetry code must be in [0, 48)")
+    perm = list(itertools.permutations((0, 1, 2)))[code // 8]
+    return perm, tuple(k for k in range(3) if (code % 8) >> k & 1)
+
+
+def _round8(shape) -> tuple:
+    return tuple(-(-int(s) // 8) * 8 for s in shape)
+
+
 def predict(net: UNet3D, activity: torch.Tensor, density: torch.Tensor, dose_conv: torch.Tensor,
             scales=None, sigma_max: float = 0.5, mu_clamp: float = 3.0, out: Optional[torch.Tensor] = None,
-            return_fallback: bool = False):
+            return_fallback: bool = False, symmetries: int = 1):
     """Corrected dose for a whole volume (device float32 tensors of one shape).
     The network runs on one crop covering the volume, its dims rounded up to
-    multiples of 8 (the overhang reads as zero input).  Everything is enqueued on
-    the current stream without a host round trip; ``net.status()`` reads the
-    tensor-core pipeline's status word afterwards."""
+    multiples of 8 (the overhang reads as zero input).  ``symmetries`` (1, 8 or 48)
+    averages the prediction (mu and s) over that many grid symmetries: the network
+    runs on each transformed volume and its output is mapped back and summed
+    (pvd_unet_symmetry_accumulate).  The 8 flips hold for any voxel size; the 48
+    include axis permutations and hold only for isotropic voxels.  Everything is
+    enqueued on the current stream without a host round trip; ``net.status()``
+    reads the tensor-core pipeline's status word afterwards."""
+    if symmetries not in SYMMETRY_SETS:
+        raise ValueError(f"symmetries must be one of {SYMMETRY_SETS}")
     dev = net.device
     shape = tuple(activity.shape)
     if scales is None:
@@ -537,11 +628,23 @@ def predict(net: UNet3D, activity: torch.Tensor, density: torch.Tensor, dose_con
         out = torch.empty(shape, dtype=torch.float32, device=dev)
     fb = torch.empty(shape, dtype=torch.uint8, device=dev) if return_fallback else None
     stream = _stream_handle(None)
-    crop = tuple(-(-s // 8) * 8 for s in shape)
+    crop = _round8(shape)
     ws = net.workspace(crop, train=False)
-    net.pack_input(ws, (activity, density, dose_conv), scales, (0, 0, 0), stream)
-    pred = net.forward(ws, stream)
+    vols = (activity, density, dose_conv)
     vd = (C.c_int * 3)(*shape)
+    if symmetries == 1:
+        net.pack_input(ws, vols, scales, (0, 0, 0), stream)
+        pred = net.forward(ws, stream)
+    else:
+        pred = net._sym_buffer(crop)
+        for k in range(symmetries):
+            perm, _ = symmetry(k)
+            ws_k = net.workspace(_round8(shape[a] for a in perm), train=False)
+            net.pack_input(ws_k, vols, scales, (0, 0, 0), stream, sym=k)
+            pk = net.forward(ws_k, stream)
+            N.check(net._lib.pvd_unet_symmetry_accumulate(C.byref(ws_k.geo[0]), pk.data_ptr(), C.byref(ws.geo[0]),
+                                                          vd, k, 1.0 / symmetries, int(k > 0), pred.data_ptr(),
+                                                          stream))
     org = (C.c_int * 3)(0, 0, 0)
     N.check(net._lib.pvd_unet_apply_correction(C.byref(ws.geo[0]), pred.data_ptr(), dose_conv.data_ptr(), vd, org,
                                                sigma_max, mu_clamp, out.data_ptr(),
@@ -584,7 +687,9 @@ class NNCorrectedDoseCalculator(DosimetryCalculator):
     correction, behind the reference's calculator interface
     (core/dosimetry_base.py:8-70).  config: ``model`` (a UNet3D) or
     ``model_path`` (.npz from save_model), ``sigma_max`` (fallback threshold on
-    the predicted error of log(D_MC/D_conv), default 0.5), plus the
+    the predicted error of log(D_MC/D_conv), default 0.5), ``symmetries`` (the
+    prediction averaged over the 8 grid flips by default; 48 adds the axis
+    permutations and needs isotropic voxels; 1 runs the network once), plus the
     convolution calculator's own options.  The convolution runs under
     ``mc_consistent_config`` (the energy per decay of the Monte Carlo the network
     was trained against) unless the config says otherwise.  Without a density map
@@ -606,6 +711,9 @@ class NNCorrectedDoseCalculator(DosimetryCalculator):
             raise ValueError("NNCorrectedDoseCalculator needs config['model'] or config['model_path']")
         self.model: UNet3D = model
         self.sigma_max = float(self.config.get("sigma_max", 0.5))
+        self.symmetries = int(self.config.get("symmetries", 8))
+        if self.symmetries not in SYMMETRY_SETS:
+            raise ValueError(f"symmetries must be one of {SYMMETRY_SETS}")
         self._fb = None
 
     def calculate_dose_rate(self, activity_map, voxel_size: Tuple[float, float, float], density=None):
@@ -617,9 +725,12 @@ class NNCorrectedDoseCalculator(DosimetryCalculator):
         a = _io.to_device(activity_map, dev, "activity")
         if density is None:
             return _io.from_device(self.conv.calculate_dose_rate(a, voxel_size), kind)
+        if self.symmetries == 48 and len({float(v) for v in voxel_size}) != 1:
+            raise ValueError("48 symmetries (axis permutations) need isotropic voxels; use 8")
         rho = _io.to_device(density, dev, "density")
         dc = self.conv.calculate_dose_rate(a, voxel_size, density=rho)
-        out, self._fb = predict(self.model, a, rho, dc, sigma_max=self.sigma_max, return_fallback=True)
+        out, self._fb = predict(self.model, a, rho, dc, sigma_max=self.sigma_max, return_fallback=True,
+                                symmetries=self.symmetries)
         self.model.status()
         return _io.from_device(out, kind)
 

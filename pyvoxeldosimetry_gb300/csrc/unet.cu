@@ -729,14 +729,43 @@ __device__ __forceinline__ long long row_of(const Geo& g, int z, int y, int x) {
   return g.margin + ((long long)(z + 1) * g.Hp + (y + 1)) * g.Wp + (x + 1);
 }
 
+// Grid symmetry: U = flip(transpose(V, perm), flips).  U's axis k is V's axis perm[k],
+// read backwards when flip[k]; U's dims are V's dims permuted.
+struct Sym {
+  int perm[3], flip[3];
+};
+
+__host__ __device__ inline Sym sym_of(int code) {
+  Sym t;
+  const int p = code / 8, f = code % 8;
+  // the six permutations of (0, 1, 2) in lexicographic order
+  t.perm[0] = p / 2;
+  const int r0 = p / 2 == 0 ? 1 : 0, r1 = p / 2 == 2 ? 1 : 2;  // the two axes left, ascending
+  t.perm[1] = (p & 1) ? r1 : r0;
+  t.perm[2] = (p & 1) ? r0 : r1;
+  for (int k = 0; k < 3; ++k) t.flip[k] = (f >> k) & 1;
+  return t;
+}
+
+// V-coordinate of U's point u along V's axes: v[perm[k]] = flip[k] ? dim - 1 - u[k] : u[k]
+__device__ __forceinline__ void sym_to_v(const Sym& t, const int* vdim, const int u[3], int v[3]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int ax = t.perm[k];
+    v[ax] = t.flip[k] ? vdim[ax] - 1 - u[k] : u[k];
+  }
+}
+
 // network input: channel c of the first n_in volumes (float32, C order, full grid
-// vd x vh x vw) read at origin + voxel, transformed, others zero
+// vd x vh x vw) read at origin + voxel of the transformed volume U, scaled and
+// mapped, others zero
 struct InputArgs {
   const float* vol[4];
   float scale[4];
   const float* scale_d;  // device scales (n_in floats) overriding scale[], or null
   int mode[4];
   int n_in, origin[3], vdim[3];
+  Sym sym;
   uint8_t* x;
   long long plane;
   Geo g;
@@ -747,9 +776,13 @@ __global__ void k_pack_input(const InputArgs a) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int x = (int)(i % a.g.W), y = (int)((i / a.g.W) % a.g.H), z = (int)(i / ((long long)a.g.W * a.g.H));
-  const int sz = z + a.origin[0], sy = y + a.origin[1], sx = x + a.origin[2];
-  const bool inside = sz >= 0 && sz < a.vdim[0] && sy >= 0 && sy < a.vdim[1] && sx >= 0 && sx < a.vdim[2];
-  const long long src = inside ? ((long long)sz * a.vdim[1] + sy) * a.vdim[2] + sx : 0;
+  const int u[3] = {z + a.origin[0], y + a.origin[1], x + a.origin[2]};
+  bool inside = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) inside = inside && u[k] >= 0 && u[k] < a.vdim[a.sym.perm[k]];
+  int v[3] = {0, 0, 0};
+  if (inside) sym_to_v(a.sym, a.vdim, u, v);
+  const long long src = inside ? ((long long)v[0] * a.vdim[1] + v[1]) * a.vdim[2] + v[2] : 0;
   float f[16];
 #pragma unroll
   for (int c = 0; c < 16; ++c) f[c] = 0.f;
@@ -1000,6 +1033,31 @@ __global__ void k_apply(const float* __restrict__ pred, Geo g, const float* __re
   const bool fb = !(expf(0.5f * pred[n + i]) <= sigma_max);
   out[v] = fb ? dose[v] : dose[v] * expf(mu);
   if (fallback) fallback[v] = fb ? 1 : 0;
+}
+
+// pred_avg[c][v] (+)= w * pred_sym[c][T(v)] over the voxels v of V (dims vd), T(v) in
+// U = flip(transpose(V, perm)); both predictions dense [2][crop dims] at origin 0
+__global__ void k_sym_accumulate(const float* __restrict__ ps, Geo gs, float* __restrict__ acc, Geo g, int vd0,
+                                 int vd1, int vd2, Sym t, float w, int accumulate) {
+  const long long n = (long long)vd0 * vd1 * vd2;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int v[3] = {(int)(i / ((long long)vd1 * vd2)), (int)((i / vd2) % vd1), (int)(i % vd2)};
+  const int vdim[3] = {vd0, vd1, vd2};
+  int u[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int ax = t.perm[k];
+    u[k] = t.flip[k] ? vdim[ax] - 1 - v[ax] : v[ax];
+  }
+  const long long ns = (long long)gs.D * gs.H * gs.W, na = (long long)g.D * g.H * g.W;
+  const long long is = ((long long)u[0] * gs.H + u[1]) * gs.W + u[2];
+  const long long ia = ((long long)v[0] * g.H + v[1]) * g.W + v[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const float val = w * ps[c * ns + is];
+    acc[c * na + ia] = accumulate ? acc[c * na + ia] + val : val;
+  }
 }
 
 // maxima[0] = max activity, maxima[1] = max dose over voxels with density >= rho_min
@@ -1268,7 +1326,17 @@ extern "C" pvd_status pvd_unet_conv3d_wgrad(const pvd_unet_geom* geom, const voi
   a.plane = a.geo.rows * 16;
   const size_t st_bytes = 16 * WG_KT * 16 + (size_t)(cout / 8) * WG_KT * 16;
   const size_t smem = (size_t)a.ns * st_bytes + (2 * a.ns + 1) * 8 + 16;
-  PVD_CUDA_TRY(cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  {
+    // raised only when a larger stage ring is needed: after the first call per layer shape no
+    // attribute call remains, so a training step can be captured in a CUDA graph
+    static size_t smem_set = 0;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lock(mu);
+    if (smem > smem_set) {
+      PVD_CUDA_TRY(cudaFuncSetAttribute(k_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      smem_set = smem;
+    }
+  }
   k_wgrad<<<dim3(a.m_tiles, a.splits), CONV_THREADS, smem, (cudaStream_t)stream>>>(a);
   PVD_LAUNCH_CHECK("k_wgrad");
   const int total = cout * cin * 27;
@@ -1294,12 +1362,21 @@ extern "C" pvd_status pvd_unet_pack_weights(const float* w, int cin, int cout, v
 extern "C" pvd_status pvd_unet_pack_input(const pvd_unet_geom* geom, const float* const* volumes, const float* scales,
                                           const float* scales_d, const int* modes, int n_in, const int* vol_dims,
                                           const int* origin, void* x, pvd_stream stream) {
+  return pvd_unet_pack_input_sym(geom, volumes, scales, scales_d, modes, n_in, vol_dims, origin, 0, x, stream);
+}
+
+extern "C" pvd_status pvd_unet_pack_input_sym(const pvd_unet_geom* geom, const float* const* volumes,
+                                              const float* scales, const float* scales_d, const int* modes, int n_in,
+                                              const int* vol_dims, const int* origin, int sym, void* x,
+                                              pvd_stream stream) {
   pvd_status st = geo_check(geom);
   if (st != PVD_OK) return st;
   if (n_in < 1 || n_in > 4 || !volumes || (!scales && !scales_d) || !modes || !vol_dims || !origin || !x || !al16(x))
     return set_error(PVD_ERR_ARG, "pvd_unet_pack_input: bad arguments");
+  if (sym < 0 || sym >= PVD_UNET_SYMMETRIES) return set_error(PVD_ERR_ARG, "pvd_unet_pack_input_sym: sym out of range");
   InputArgs a;
   a.g = make_geo(geom);
+  a.sym = sym_of(sym);
   for (int i = 0; i < 3; ++i) {
     a.origin[i] = origin[i];
     a.vdim[i] = vol_dims[i];
@@ -1459,6 +1536,27 @@ extern "C" pvd_status pvd_unet_bias_grad(const pvd_unet_geom* geom, const void* 
   PVD_LAUNCH_CHECK("k_bias_grad");
   k_sum_rows<<<channels, 256, 0, (cudaStream_t)stream>>>((const float*)workspace, (int)nblk, channels, db);
   PVD_LAUNCH_CHECK("k_sum_rows");
+  return PVD_OK;
+}
+
+extern "C" pvd_status pvd_unet_symmetry_accumulate(const pvd_unet_geom* geom_sym, const float* pred_sym,
+                                                   const pvd_unet_geom* geom, const int* vol_dims, int sym,
+                                                   float weight, int accumulate, float* pred_avg, pvd_stream stream) {
+  pvd_status st = geo_check(geom_sym);
+  if (st == PVD_OK) st = geo_check(geom);
+  if (st != PVD_OK) return st;
+  if (!pred_sym || !pred_avg || !vol_dims || sym < 0 || sym >= PVD_UNET_SYMMETRIES || !std::isfinite(weight))
+    return set_error(PVD_ERR_ARG, "pvd_unet_symmetry_accumulate: bad arguments");
+  const Geo gs = make_geo(geom_sym), g = make_geo(geom);
+  const Sym t = sym_of(sym);
+  const int cs[3] = {gs.D, gs.H, gs.W}, ca[3] = {g.D, g.H, g.W};
+  for (int k = 0; k < 3; ++k)
+    if (vol_dims[k] < 1 || vol_dims[k] > ca[k] || vol_dims[t.perm[k]] > cs[k])
+      return set_error(PVD_ERR_ARG, "pvd_unet_symmetry_accumulate: a crop does not cover its volume");
+  const long long n = (long long)vol_dims[0] * vol_dims[1] * vol_dims[2];
+  k_sym_accumulate<<<blocks_for(n, 256), 256, 0, (cudaStream_t)stream>>>(
+      pred_sym, gs, pred_avg, g, vol_dims[0], vol_dims[1], vol_dims[2], t, weight, accumulate ? 1 : 0);
+  PVD_LAUNCH_CHECK("k_sym_accumulate");
   return PVD_OK;
 }
 

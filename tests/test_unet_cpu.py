@@ -114,16 +114,33 @@ def test_dose_errors_restricts_to_tissue_above_threshold():
 
 
 def test_log_ratio_target():
-    dc = np.array([10.0, 5.0, 0.5, 8.0, 4.0, 100.0])
-    dm = np.array([12.0, 5.0, 0.6, 0.0, 4.0 * np.e ** 5, 1.0])
-    rho = np.array([1.0, 0.3, 1.0, 1.0, 1.85, 0.0012])  # last voxel is air
+    dc = np.array([10.0, 5.0, 0.5, 8.0, 4.0, 100.0, 0.9, 0.3])
+    dm = np.array([12.0, 5.0, 0.6, 0.0, 4.0 * np.e ** 5, 1.0, 600.0, 59.0])
+    rho = np.array([1.0, 0.3, 1.0, 1.0, 1.85, 0.0012, 0.3, 0.3])  # voxel 5 is air
     t, w, dmax = lc.log_ratio_target(dc, dm, rho, rel_threshold=0.1)
     assert dmax == 10.0  # the air voxel's 100 is not a tissue maximum
-    # weighted: tissue, conv dose > 1.0, both doses positive
-    assert w.tolist() == [1.0, 1.0, 0.0, 0.0, 1.0, 0.0]
+    # weighted: tissue with conv dose > 1.0 or MC dose > 60.0 (10 % of 600), both doses positive
+    assert w.tolist() == [1.0, 1.0, 0.0, 0.0, 1.0, 0.0, 1.0, 0.0]
     assert t[0] == pytest.approx(np.log(1.2)) and t[1] == 0.0
     assert t[4] == pytest.approx(3.0)  # clipped
+    assert t[6] == pytest.approx(3.0)  # selected on the MC dose alone (lung), clipped
     assert t.dtype == np.float32 and w.dtype == np.float32
+
+
+def test_focused_crops_hold_a_weighted_voxel_and_stay_in_range():
+    rng = np.random.default_rng(0)
+    for _ in range(3000):
+        vd = tuple(int(x) for x in rng.integers(20, 140, 3))
+        crop = tuple(int(x) for x in rng.choice([32, 48, 64], 3))
+        w = rng.random(vd) > 0.999
+        hot = np.flatnonzero(w.ravel())
+        o = lc.crop_origin(rng, vd, crop, hot)
+        assert all(min(0, vd[k] - crop[k]) <= o[k] <= max(0, vd[k] - crop[k]) for k in range(3))
+        if hot.size:
+            sub = w[max(o[0], 0):o[0] + crop[0], max(o[1], 0):o[1] + crop[1], max(o[2], 0):o[2] + crop[2]]
+            assert sub.any()
+        o2 = lc.crop_origin(rng, vd, crop)          # unfocused: the same range
+        assert all(min(0, vd[k] - crop[k]) <= o2[k] <= max(0, vd[k] - crop[k]) for k in range(3))
 
 
 def test_every_bulk_copy_stays_inside_the_plane():

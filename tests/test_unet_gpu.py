@@ -390,3 +390,29 @@ def test_gradient_clip_and_running_mean_limit():
     torch.cuda.synchronize()
     assert float(g4.abs().max()) == 0.0 and not torch.isnan(g4).any() and float(work[1027]) == 2.0
     assert lib.pvd_grad_clip(g.data_ptr(), g.numel(), 0.0, 1.0, work.data_ptr(), None) == 1
+
+
+def test_graph_replayed_training_matches_eager(env):
+    """train(graphs=True) replays the forward pass and the layer backward as CUDA
+    graphs; every reduction in a step has a fixed order, so the parameters after a few
+    steps equal those of the eager loop bit for bit (focused crops, a crop that fits)."""
+    N, lc, lib, dev = env
+    shape = (24, 32, 24)
+    rng = np.random.default_rng(8)
+    act = rng.random(shape).astype(np.float32)
+    rho = (0.3 + rng.random(shape)).astype(np.float32)
+    dc = (act * 0.01 + 1e-3).astype(np.float32)
+    dm = (dc * np.exp(rng.normal(0.0, 0.1, shape))).astype(np.float32)
+    pair = lc.make_pair(act, rho, dc, dm, device=dev)
+    nets = []
+    for graphs in (False, True):
+        net = lc.UNet3D(seed=2, device=dev)
+        lc.train(net, [pair], 6, crop=(16, 16, 16), lr=1e-3, seed=1, graphs=graphs)
+        net.status()
+        nets.append(net)
+    assert torch.equal(nets[0].params, nets[1].params)
+    assert not torch.equal(nets[0].params, lc.UNet3D(seed=2, device=dev).params)   # the steps did move them
+    # inference after graph training packs the final weights
+    a, r, d = (torch.from_numpy(x).to(dev) for x in (act, rho, dc))
+    assert torch.equal(lc.predict(nets[0], a, r, d, sigma_max=float("inf")),
+                       lc.predict(nets[1], a, r, d, sigma_max=float("inf")))
