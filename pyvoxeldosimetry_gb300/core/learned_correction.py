@@ -195,8 +195,9 @@ class UNet3D:
         self.packed_bwd = torch.zeros(po, dtype=torch.bfloat16, device=self.device)
         self.clip_work = torch.zeros(1028, dtype=torch.float32, device=self.device)
         self.step = 0
-        self._ws: Dict[Tuple[Tuple[int, int, int], bool], _Workspace] = {}
+        self._ws: Dict[Tuple[Tuple[int, int, int], bool, int], _Workspace] = {}
         self._sym: Dict[Tuple[int, int, int], torch.Tensor] = {}
+        self._side: List[torch.cuda.Stream] = []
         self._packed_for = -1
 
     # --- parameters -------------------------------------------------------
@@ -234,12 +235,19 @@ class UNet3D:
             buf = self._sym[crop] = torch.empty(2 * int(np.prod(crop)), dtype=torch.float32, device=self.device)
         return buf
 
-    def workspace(self, dims, train: bool) -> _Workspace:
-        key = (tuple(int(d) for d in dims), bool(train))
+    def workspace(self, dims, train: bool, slot: int = 0) -> _Workspace:
+        """The activations of one crop shape (slot: one per stream that runs passes
+        concurrently)."""
+        key = (tuple(int(d) for d in dims), bool(train), int(slot))
         ws = self._ws.get(key)
         if ws is None:
             ws = self._ws[key] = _Workspace(dims, self.device, train)
         return ws
+
+    def side_streams(self, n: int) -> List[torch.cuda.Stream]:
+        while len(self._side) < n:
+            self._side.append(torch.cuda.Stream(self.device))
+        return self._side[:n]
 
     # --- layers -----------------------------------------------------------
     def _conv(self, name, x: _Tensor, y: _Tensor, stream) -> None:
@@ -606,18 +614,32 @@ def _round8(shape) -> tuple:
     return tuple(-(-int(s) // 8) * 8 for s in shape)
 
 
+INFERENCE_BYTES_PER_VOXEL = 300  # activations of every level (BF16) + the FP32 prediction, per crop voxel
+
+
+def flip_streams(symmetries: int, crop, device) -> int:
+    """How many symmetry passes run concurrently: up to 4, each with its own
+    workspace, within a quarter of the device's free memory."""
+    free, _ = torch.cuda.mem_get_info(device)
+    per = INFERENCE_BYTES_PER_VOXEL * int(np.prod(crop))
+    return max(1, min(4, symmetries, int(0.25 * free) // max(per, 1)))
+
+
 def predict(net: UNet3D, activity: torch.Tensor, density: torch.Tensor, dose_conv: torch.Tensor,
             scales=None, sigma_max: float = 0.5, mu_clamp: float = 3.0, out: Optional[torch.Tensor] = None,
-            return_fallback: bool = False, symmetries: int = 1):
+            return_fallback: bool = False, symmetries: int = 1, streams: Optional[int] = None):
     """Corrected dose for a whole volume (device float32 tensors of one shape).
     The network runs on one crop covering the volume, its dims rounded up to
     multiples of 8 (the overhang reads as zero input).  ``symmetries`` (1, 8 or 48)
     averages the prediction (mu and s) over that many grid symmetries: the network
     runs on each transformed volume and its output is mapped back and summed
     (pvd_unet_symmetry_accumulate).  The 8 flips hold for any voxel size; the 48
-    include axis permutations and hold only for isotropic voxels.  Everything is
-    enqueued on the current stream without a host round trip; ``net.status()``
-    reads the tensor-core pipeline's status word afterwards."""
+    include axis permutations and hold only for isotropic voxels.  The passes run on
+    ``streams`` side streams at once (default ``flip_streams``: the deep, small layers
+    of one pass leave most SMs idle), and are summed on the current stream in
+    symmetry order, so the result does not depend on the stream count.  Everything
+    is enqueued without a host round trip; the current stream waits for all of it.
+    ``net.status()`` reads the tensor-core pipeline's status word afterwards."""
     if symmetries not in SYMMETRY_SETS:
         raise ValueError(f"symmetries must be one of {SYMMETRY_SETS}")
     dev = net.device
@@ -629,24 +651,41 @@ def predict(net: UNet3D, activity: torch.Tensor, density: torch.Tensor, dose_con
     fb = torch.empty(shape, dtype=torch.uint8, device=dev) if return_fallback else None
     stream = _stream_handle(None)
     crop = _round8(shape)
-    ws = net.workspace(crop, train=False)
+    geo0 = geometry(crop)
     vols = (activity, density, dose_conv)
     vd = (C.c_int * 3)(*shape)
     if symmetries == 1:
+        ws = net.workspace(crop, train=False)
         net.pack_input(ws, vols, scales, (0, 0, 0), stream)
         pred = net.forward(ws, stream)
     else:
         pred = net._sym_buffer(crop)
+        main = torch.cuda.current_stream(dev)
+        net._pack(stream)  # weights packed once, before the passes fork
+        nst = streams if streams is not None else flip_streams(symmetries, crop, dev)
+        side = net.side_streams(max(1, min(int(nst), symmetries)))
+        ready = torch.cuda.Event()
+        ready.record(main)
+        reusable = [ready] * len(side)  # when a side stream's workspace may be written again
         for k in range(symmetries):
+            i = k % len(side)
+            st = side[i]
+            st.wait_event(reusable[i])
             perm, _ = symmetry(k)
-            ws_k = net.workspace(_round8(shape[a] for a in perm), train=False)
-            net.pack_input(ws_k, vols, scales, (0, 0, 0), stream, sym=k)
-            pk = net.forward(ws_k, stream)
-            N.check(net._lib.pvd_unet_symmetry_accumulate(C.byref(ws_k.geo[0]), pk.data_ptr(), C.byref(ws.geo[0]),
+            ws_k = net.workspace(_round8(shape[a] for a in perm), train=False, slot=i + 1)
+            sh = int(st.cuda_stream)
+            net.pack_input(ws_k, vols, scales, (0, 0, 0), sh, sym=k)
+            pk = net.forward(ws_k, sh)
+            done = torch.cuda.Event()
+            done.record(st)
+            main.wait_event(done)
+            N.check(net._lib.pvd_unet_symmetry_accumulate(C.byref(ws_k.geo[0]), pk.data_ptr(), C.byref(geo0),
                                                           vd, k, 1.0 / symmetries, int(k > 0), pred.data_ptr(),
                                                           stream))
+            reusable[i] = torch.cuda.Event()
+            reusable[i].record(main)
     org = (C.c_int * 3)(0, 0, 0)
-    N.check(net._lib.pvd_unet_apply_correction(C.byref(ws.geo[0]), pred.data_ptr(), dose_conv.data_ptr(), vd, org,
+    N.check(net._lib.pvd_unet_apply_correction(C.byref(geo0), pred.data_ptr(), dose_conv.data_ptr(), vd, org,
                                                sigma_max, mu_clamp, out.data_ptr(),
                                                fb.data_ptr() if fb is not None else None, stream))
     return (out, fb) if return_fallback else out

@@ -144,6 +144,9 @@ def test_predict_averages_over_flips(setup):
     a, r = torch.from_numpy(act).to(dev), torch.from_numpy(rho).to(dev)
     dc = torch.from_numpy(np.ascontiguousarray(act * 1e-3 + 1e-4)).to(dev)
     out8 = lc.predict(net, a, r, dc, sigma_max=float("inf"), symmetries=8)
+    # the passes on 1 or 3 side streams are summed in the same order: the same dose, bit for bit
+    for n in (1, 3):
+        assert torch.equal(lc.predict(net, a, r, dc, sigma_max=float("inf"), symmetries=8, streams=n), out8)
     crop = tuple(-(-n // 8) * 8 for n in act.shape)
     mus = []
     for code in range(8):
