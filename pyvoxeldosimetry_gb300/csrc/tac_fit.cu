@@ -18,6 +18,8 @@
 // HBM traffic per voxel: 4T bytes read, 8(n_par+1)+1 bytes written; the
 // kernel is FP64-throughput bound (exp and the normal equations per iteration).
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <type_traits>
 #include <cmath>
 
@@ -1051,6 +1053,38 @@ __global__ void __launch_bounds__(kVpThreads) k_tac_fit_vp(FitArgs a, const floa
   refill_loop(r0, r1, &next, init, tick, finish);
 }
 
+// Grid of a variable-projection stage: as many blocks as the device holds at once
+// (SMs x resident blocks of the kernel, computed once per kernel), each owning an
+// equal contiguous range of voxels.
+struct VpGrid {
+  int blocks;
+  long long per_block;
+};
+
+inline VpGrid vp_grid(const void* kern, long long n_vox) {
+  static std::mutex mu;
+  static std::map<const void*, int> wave;
+  int slots = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = wave.find(kern);
+    if (it == wave.end()) {
+      int dev = 0, sms = 0, occ = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+          cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kVpThreads, 0) != cudaSuccess) {
+        cudaGetLastError();
+        sms = 152, occ = 1;
+      }
+      it = wave.emplace(kern, std::max(1, sms) * std::max(1, occ)).first;
+    }
+    slots = it->second;
+  }
+  const long long nblk = std::max(1LL, std::min<long long>((n_vox + kVpThreads - 1) / kVpThreads, slots));
+  const long long per_block = (n_vox + nblk - 1) / nblk;
+  return VpGrid{(int)((n_vox + per_block - 1) / per_block), per_block};
+}
+
 }  // namespace pvd
 
 using namespace pvd;
@@ -1095,22 +1129,23 @@ extern "C" pvd_status pvd_tac_fit(int model, const double* times, const double* 
   const int threads = 128;
   const int blocks = (int)std::min<long long>((n_vox + threads - 1) / threads, 152LL * 64);
   if (flags & PVD_FIT_VARPRO) {
-    // blocks own contiguous voxel ranges; a few blocks per SM keep the refill local
-    const long long nblk = std::min<long long>((n_vox + kVpThreads - 1) / kVpThreads, 152LL * 8);
-    const long long per_block = (n_vox + nblk - 1) / nblk;
-    const int g = (int)((n_vox + per_block - 1) / per_block);
+    // blocks own contiguous voxel ranges, one resident wave of them per launch: a block's
+    // range ends on its slowest voxel (up to max_fev evaluations on one lane), and a
+    // second wave would pay that tail again
     const int pg = (int)std::min<long long>((n_vox + kVpThreads - 1) / kVpThreads, 152LL * 32);
 #define PVD_VP_LAUNCH(MV)                                                                                   \
   {                                                                                                         \
     if (a.mixed) {                                                                                          \
-      k_tac_fit_vp<MV, 0><<<g, kVpThreads, 0, st>>>(a, acts_d, n_vox, per_block, params_d, auc_d, ok_d,     \
-                                                    auc_f32_d);                                             \
+      const VpGrid g0 = vp_grid((const void*)k_tac_fit_vp<MV, 0>, n_vox);                                   \
+      k_tac_fit_vp<MV, 0><<<g0.blocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, g0.per_block, params_d, auc_d, \
+                                                            ok_d, auc_f32_d);                               \
       PVD_LAUNCH_CHECK("k_tac_fit_vp<fp32>");                                                               \
       k_tac_fit_vp_polish<MV><<<pg, kVpThreads, 0, st>>>(a, acts_d, n_vox, params_d, auc_d, ok_d, auc_f32_d); \
       PVD_LAUNCH_CHECK("k_tac_fit_vp_polish");                                                              \
     }                                                                                                       \
-    k_tac_fit_vp<MV, 1><<<g, kVpThreads, 0, st>>>(a, acts_d, n_vox, per_block, params_d, auc_d, ok_d,       \
-                                                  auc_f32_d);                                               \
+    const VpGrid g1 = vp_grid((const void*)k_tac_fit_vp<MV, 1>, n_vox);                                     \
+    k_tac_fit_vp<MV, 1><<<g1.blocks, kVpThreads, 0, st>>>(a, acts_d, n_vox, g1.per_block, params_d, auc_d,   \
+                                                          ok_d, auc_f32_d);                                 \
     PVD_LAUNCH_CHECK("k_tac_fit_vp<fp64>");                                                                 \
   }
     if (n_times == 4)
