@@ -104,6 +104,44 @@ def byte_model(shape, kmax, nk, density):
     return m
 
 
+def link_bound(act_h, out_h, e2e_ms, passes, device_ms, reps=5):
+    """The host link's share of one end-to-end step: plain pinned copies of the activity
+    (up) and of every slot's dose (down), timed alone with CUDA events, and the
+    critical path they set: the activity upload precedes the z pass,
+    the passes after the forward ones (z, y inverse, the first inverse-x chunk) run
+    before the first dose chunk can go back, and the dose copy-back ends the step
+    (the density upload overlaps the forward passes)."""
+    import torch
+    dev = torch.device("cuda", torch.cuda.current_device())
+
+    def timed(dst, src):
+        dst.copy_(src, non_blocking=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ts = []
+        for _ in range(reps):
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    a_d = torch.empty(act_h.shape, dtype=torch.float32, device=dev)
+    o_d = torch.empty(out_h.shape, dtype=torch.float32, device=dev)
+    up_ms = timed(a_d, act_h)
+    down_ms = timed(out_h, o_d)
+    del a_d, o_d
+    mid_ms = sum(passes.get(k, 0.0) for k in ("z_fwd_mul_inv", "y_inv")) + passes.get("x_inv", 0.0) / 4
+    bound = up_ms + mid_ms + down_ms
+    return {"activity_up_ms": up_ms, "activity_up_gb_s": act_h.numel() * 4 / up_ms / 1e6,
+            "dose_down_ms": down_ms, "dose_down_gb_s": out_h.numel() * 4 / down_ms / 1e6,
+            "critical_path_ms": bound, "e2e_ms": e2e_ms, "e2e_frac_of_link_bound": bound / e2e_ms,
+            "device_resident_ms": device_ms,
+            "note": "the host link (about 200 GB/s each way on this box, copy engine or SM loads/stores alike) "
+                    "bounds the end-to-end step; the passes between the uploads and the copy-back are taken "
+                    "from this run's per-pass times"}
+
+
 def load_peaks():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -960,6 +998,8 @@ def main():
                        "d2h_bytes_per_step": 4 * vox * nk, "ms_per_step": e2e_ms / args.steps,
                        "wall_ms_per_step": 1e3 * wall / args.steps,
                        "api": "KernelConvolutionCalculator.calculate_dose_rate(pinned CPU tensors)"}
+        line["e2e"]["link"] = link_bound(act_h, out_h, e2e_ms / args.steps, roofline["pass_ms_per_step"],
+                                         total_ms / args.steps)
         if rank == 0 and not args.no_check:
             line["e2e"]["error_vs_fp64_oracle"] = oracle_errors(act, rho, wl, out_h.numpy(), refs)[0]
         # the drop-in user's call: pageable numpy in, new numpy arrays out, through the
