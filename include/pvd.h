@@ -645,6 +645,15 @@ pvd_status pvd_unet_head_loss(const pvd_unet_geom* geom, const void* x, const fl
                               const float* target, const float* weight, const int* vol_dims, const int* origin,
                               float eps, float slope, void* grad_x, float* grads_and_loss, void* workspace,
                               size_t workspace_bytes, pvd_stream stream);
+/* pvd_unet_head_loss on a crop of the transformed volumes U of grid symmetry `sym`
+ * (PVD_UNET_SYMMETRIES; origin in U's coordinates, vol_dims the untransformed dims):
+ * target and weight are read at the voxel of V the crop voxel maps to, as
+ * pvd_unet_pack_input_sym reads the inputs -- training on flipped crops.  sym 0 is
+ * pvd_unet_head_loss. */
+pvd_status pvd_unet_head_loss_sym(const pvd_unet_geom* geom, const void* x, const float* w_head, const float* pred,
+                                  const float* target, const float* weight, const int* vol_dims, const int* origin,
+                                  int sym, float eps, float slope, void* grad_x, float* grads_and_loss,
+                                  void* workspace, size_t workspace_bytes, pvd_stream stream);
 
 /* Corrected dose on the volume voxels that the crop at `origin` covers:
  * dose_out[v] = dose_conv[v] * exp(clamp(mu, +-mu_clamp)), or dose_conv[v]

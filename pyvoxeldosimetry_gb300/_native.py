@@ -50,7 +50,7 @@ EXPORTED_SYMBOLS = [
     "pvd_unet_pack_weights", "pvd_unet_pack_input", "pvd_unet_pack_input_sym", "pvd_unet_symmetry_accumulate",
     "pvd_unet_pool", "pvd_unet_pool_backward",
     "pvd_unet_upsample", "pvd_unet_upsample_backward", "pvd_unet_head", "pvd_unet_head_loss_workspace",
-    "pvd_unet_head_loss", "pvd_unet_apply_correction", "pvd_unet_input_maxima", "pvd_unet_bias_grad_workspace", "pvd_unet_bias_grad", "pvd_adam_step", "pvd_grad_clip",
+    "pvd_unet_head_loss", "pvd_unet_head_loss_sym", "pvd_unet_apply_correction", "pvd_unet_input_maxima", "pvd_unet_bias_grad_workspace", "pvd_unet_bias_grad", "pvd_adam_step", "pvd_grad_clip",
     "pvd_unet_status",
     "pvd_wait_check", "pvd_set_plan_alloc_cap",
     "pvd_last_error", "pvd_version", "pvd_launch_count",
@@ -197,6 +197,8 @@ def _declare(lib: C.CDLL) -> None:
         "pvd_unet_head_loss_workspace": (st, [C.POINTER(UnetGeom), C.POINTER(C.c_size_t)]),
         "pvd_unet_head_loss": (st, [C.POINTER(UnetGeom), vp, vp, vp, vp, vp, C.POINTER(i), C.POINTER(i), f, f, vp,
                                     vp, vp, C.c_size_t, vp]),
+        "pvd_unet_head_loss_sym": (st, [C.POINTER(UnetGeom), vp, vp, vp, vp, vp, C.POINTER(i), C.POINTER(i), i, f,
+                                        f, vp, vp, vp, C.c_size_t, vp]),
         "pvd_unet_apply_correction": (st, [C.POINTER(UnetGeom), vp, vp, C.POINTER(i), C.POINTER(i), f, f, vp, vp,
                                            vp]),
         "pvd_unet_input_maxima": (st, [vp, vp, vp, C.c_int64, f, vp, vp]),

@@ -329,17 +329,19 @@ class UNet3D:
         self.head_loss(ws, target, weight, origin, stream)
         self.backward_layers(ws, stream)
 
-    def head_loss(self, ws: _Workspace, target: torch.Tensor, weight: torch.Tensor, origin, stream) -> None:
-        """The loss, the head's gradients and the gradient into the last layer."""
+    def head_loss(self, ws: _Workspace, target: torch.Tensor, weight: torch.Tensor, origin, stream,
+                  sym: int = 0) -> None:
+        """The loss, the head's gradients and the gradient into the last layer (``sym``:
+        the crop is of the volumes transformed by that grid symmetry, as packed)."""
         if not ws.gr:
             raise RuntimeError("workspace was created for inference only")
         t, gr, lib = ws.t, ws.gr, self._lib
         vd = (C.c_int * 3)(*[int(d) for d in target.shape])
         org = (C.c_int * 3)(*[int(o) for o in origin])
-        N.check(lib.pvd_unet_head_loss(C.byref(ws.geo[0]), t["d0b"].ptr, self._ptr(self.params, self.head_offset),
-                                       ws.pred.data_ptr(), target.data_ptr(), weight.data_ptr(), vd, org, EPS, SLOPE,
-                                       gr["d0b"].ptr, self._ptr(self.grads, self.head_offset),
-                                       ws.scratch.data_ptr(), ws.scratch.numel(), stream))
+        N.check(lib.pvd_unet_head_loss_sym(C.byref(ws.geo[0]), t["d0b"].ptr, self._ptr(self.params, self.head_offset),
+                                           ws.pred.data_ptr(), target.data_ptr(), weight.data_ptr(), vd, org, int(sym),
+                                           EPS, SLOPE, gr["d0b"].ptr, self._ptr(self.grads, self.head_offset),
+                                           ws.scratch.data_ptr(), ws.scratch.numel(), stream))
 
     def backward_layers(self, ws: _Workspace, stream) -> None:
         """Every layer's parameter gradients, from the gradient head_loss left in the
@@ -518,28 +520,37 @@ def generate_training_pairs(n: int, shape=(64, 64, 64), voxel_mm: float = 4.0, r
     return pairs
 
 
-def crop_origin(rng: np.random.Generator, vd, crop, hot: Optional[np.ndarray] = None) -> List[int]:
+def crop_origin(rng: np.random.Generator, vd, crop, hot: Optional[np.ndarray] = None, flips=()) -> List[int]:
     """Origin of a training crop of a volume of dims vd: inside the volume where the
     crop fits, else covering it (origin in [vd - crop, 0]).  With ``hot`` (flat indices
     of weighted voxels) the crop holds one of them, drawn uniformly, at a uniformly
-    random place within the crop, clamped to the same range (which keeps it inside)."""
+    random place within the crop, clamped to the same range (which keeps it inside).
+    ``flips``: the crop is of the volume flipped along those axes (the origin is in
+    the flipped frame; the weighted voxel is mapped into it)."""
     lo = [min(0, vd[k] - c) for k, c in enumerate(crop)]
     hi = [max(0, vd[k] - c) for k, c in enumerate(crop)]
     if hot is not None and hot.size:
-        v = np.unravel_index(int(hot[int(rng.integers(hot.size))]), vd)
-        return [min(max(int(v[k]) - int(rng.integers(c)), lo[k]), hi[k]) for k, c in enumerate(crop)]
+        v = [int(x) for x in np.unravel_index(int(hot[int(rng.integers(hot.size))]), vd)]
+        for k in flips:
+            v[k] = vd[k] - 1 - v[k]
+        return [min(max(v[k] - int(rng.integers(c)), lo[k]), hi[k]) for k, c in enumerate(crop)]
     return [int(rng.integers(lo[k], hi[k] + 1)) for k in range(3)]
 
 
 def train(net: UNet3D, pairs: Sequence[TrainingPair], steps: int, crop=(32, 32, 32), lr: float = 2e-3,
           seed: int = 0, log_every: int = 0, clip: float = 1.0, warmup: float = 0.05,
-          spike_factor: float = 10.0, focus: bool = True, graphs: bool = True) -> TrainStats:
+          spike_factor: float = 10.0, focus: bool = True, graphs: bool = True,
+          augment: bool = True) -> TrainStats:
     """Adam on random crops of random pairs; a crop lies inside its volume when it
     fits, else covers it from a random offset.  With ``focus`` every crop holds a
     weighted voxel drawn uniformly from the pair's weighted voxels, at a uniformly
     random place in the crop: the loss lives on a few tenths of a percent of the
     voxels (tissue near the activity), and a crop without any gives a zero gradient
-    that Adam's momentum still steps on.  The learning rate rises linearly over
+    that Adam's momentum still steps on.  With ``augment`` each crop is taken from the
+    volumes flipped along a random set of axes (one of the 8 flips; the inputs, target
+    and weight alike, pvd_unet_pack_input_sym / pvd_unet_head_loss_sym): the dose
+    physics is flip-invariant, and the network learns it that way instead of from the
+    phantoms' orientation.  The learning rate rises linearly over
     the first ``warmup`` fraction of the steps, then decays on a cosine; gradients are
     clipped to a global norm of ``clip`` (0: no clipping) and to ``spike_factor`` times
     the running mean of the earlier norms: one outlying crop would otherwise throw
@@ -560,15 +571,17 @@ def train(net: UNet3D, pairs: Sequence[TrainingPair], steps: int, crop=(32, 32, 
     for it in range(steps):
         ip = int(rng.integers(len(pairs)))
         p = pairs[ip]
-        origin = crop_origin(rng, tuple(p.activity.shape), crop, hot[ip])
-        net.pack_input(ws, (p.activity, p.density, p.dose_conv), p.scales, origin, stream)
+        sym = int(rng.integers(8)) if augment else 0
+        origin = crop_origin(rng, tuple(p.activity.shape), crop, hot[ip], symmetry(sym)[1])
+        net.pack_input(ws, (p.activity, p.density, p.dose_conv), p.scales, origin, stream, sym=sym)
         if g_fwd is not None:
             g_fwd.replay()
-            net.head_loss(ws, p.target, p.weight, origin, stream)
+            net.head_loss(ws, p.target, p.weight, origin, stream, sym=sym)
             g_bwd.replay()
         else:
             net.forward(ws, stream)
-            net.backward(ws, p.target, p.weight, origin, stream)
+            net.head_loss(ws, p.target, p.weight, origin, stream, sym=sym)
+            net.backward_layers(ws, stream)
         nw = max(1, int(warmup * steps))
         lr_t = lr * (it + 1) / nw if it < nw else lr * 0.5 * (1 + math.cos(math.pi * (it - nw) / max(1, steps - nw)))
         if clip > 0:

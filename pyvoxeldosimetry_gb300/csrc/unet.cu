@@ -919,8 +919,8 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_head_loss(const uint8_t* __res
                                                            const float* __restrict__ w, const float* __restrict__ pred,
                                                            const float* __restrict__ target,
                                                            const float* __restrict__ weight, int o0, int o1, int o2,
-                                                           int vd, int vh, int vw, float inv_n, float eps, float slope,
-                                                           uint8_t* gx, float* __restrict__ part) {
+                                                           int vd, int vh, int vw, Sym t_sym, float inv_n, float eps,
+                                                           float slope, uint8_t* gx, float* __restrict__ part) {
   __shared__ float red[HEAD_THREADS / 32][36];
   const long long n = (long long)g.D * g.H * g.W;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -929,9 +929,15 @@ __global__ void __launch_bounds__(HEAD_THREADS) k_head_loss(const uint8_t* __res
   for (int j = 0; j < 36; ++j) acc[j] = 0.f;
   if (i < n) {
     const int xx = (int)(i % g.W), y = (int)((i / g.W) % g.H), z = (int)(i / ((long long)g.W * g.H));
-    const int sz = z + o0, sy = y + o1, sx = xx + o2;
-    const bool inside = sz >= 0 && sz < vd && sy >= 0 && sy < vh && sx >= 0 && sx < vw;
-    const long long src = inside ? ((long long)sz * vh + sy) * vw + sx : 0;
+    // crop voxel -> point u of the transformed volume U -> voxel v of the target volumes
+    const int u[3] = {z + o0, y + o1, xx + o2};
+    const int vdim[3] = {vd, vh, vw};
+    bool inside = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) inside = inside && u[k] >= 0 && u[k] < vdim[t_sym.perm[k]];
+    int v[3] = {0, 0, 0};
+    if (inside) sym_to_v(t_sym, vdim, u, v);
+    const long long src = inside ? ((long long)v[0] * vh + v[1]) * vw + v[2] : 0;
     const float t = inside ? target[src] : 0.f, wt = inside ? weight[src] : 0.f;
     const float mu = pred[i], s = pred[n + i];
     const float e = mu - t;
@@ -1490,11 +1496,21 @@ extern "C" pvd_status pvd_unet_head_loss(const pvd_unet_geom* geom, const void* 
                                          const int* vol_dims, const int* origin, float eps, float slope, void* grad_x,
                                          float* grads_and_loss, void* workspace, size_t workspace_bytes,
                                          pvd_stream stream) {
+  return pvd_unet_head_loss_sym(geom, x, w_head, pred, target, weight, vol_dims, origin, 0, eps, slope, grad_x,
+                                grads_and_loss, workspace, workspace_bytes, stream);
+}
+
+extern "C" pvd_status pvd_unet_head_loss_sym(const pvd_unet_geom* geom, const void* x, const float* w_head,
+                                             const float* pred, const float* target, const float* weight,
+                                             const int* vol_dims, const int* origin, int sym, float eps, float slope,
+                                             void* grad_x, float* grads_and_loss, void* workspace,
+                                             size_t workspace_bytes, pvd_stream stream) {
   pvd_status st = geo_check(geom);
   if (st != PVD_OK) return st;
   if (!x || !w_head || !pred || !target || !weight || !vol_dims || !origin || !grad_x || !grads_and_loss ||
       !workspace || !al16(x) || !al16(grad_x))
     return set_error(PVD_ERR_ARG, "pvd_unet_head_loss: bad arguments");
+  if (sym < 0 || sym >= PVD_UNET_SYMMETRIES) return set_error(PVD_ERR_ARG, "pvd_unet_head_loss_sym: sym out of range");
   for (int i = 0; i < 3; ++i)
     if (vol_dims[i] < 1) return set_error(PVD_ERR_ARG, "pvd_unet_head_loss: bad volume dims");
   const Geo g = make_geo(geom);
@@ -1504,7 +1520,8 @@ extern "C" pvd_status pvd_unet_head_loss(const pvd_unet_geom* geom, const void* 
     return set_error(PVD_ERR_ARG, "pvd_unet_head_loss: workspace smaller than pvd_unet_head_loss_workspace");
   k_head_loss<<<nblk, HEAD_THREADS, 0, (cudaStream_t)stream>>>(
       (const uint8_t*)x, g.rows * 16, g, w_head, pred, target, weight, origin[0], origin[1], origin[2], vol_dims[0],
-      vol_dims[1], vol_dims[2], (float)(1.0 / (double)n), eps, slope, (uint8_t*)grad_x, (float*)workspace);
+      vol_dims[1], vol_dims[2], sym_of(sym), (float)(1.0 / (double)n), eps, slope, (uint8_t*)grad_x,
+      (float*)workspace);
   PVD_LAUNCH_CHECK("k_head_loss");
   k_sum_rows<<<36, 256, 0, (cudaStream_t)stream>>>((const float*)workspace, (int)nblk, 36, grads_and_loss);
   PVD_LAUNCH_CHECK("k_sum_rows");

@@ -166,3 +166,33 @@ def test_predict_averages_over_flips(setup):
     net.status()
     with pytest.raises(ValueError):
         lc.predict(net, a, r, dc, symmetries=4)
+
+
+def test_head_loss_sym_reads_targets_in_the_flipped_frame(setup):
+    """pvd_unet_head_loss_sym on a crop of the flipped volumes equals
+    pvd_unet_head_loss on numpy's flipped copies (inputs, target and weight), bit for
+    bit: the loss, the head's gradients and the gradient into the last layer."""
+    lc, net, path, act, rho = setup
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(11)
+    vd = (12, 18, 20)
+    vols = [rng.random(vd).astype(np.float32) for _ in range(3)]
+    tgt = rng.normal(0.0, 0.3, vd).astype(np.float32)
+    wgt = (rng.random(vd) > 0.4).astype(np.float32)
+    s = torch.cuda.current_stream().cuda_stream
+    ws = net.workspace((16, 16, 16), train=True)
+    origin = (-2, 1, 3)
+    for code in (3, 5, 6):
+        _, flips = lc.symmetry(code)
+        outs = []
+        for sym, vv, tt, ww in ((code, vols, tgt, wgt),
+                                (0, [np.ascontiguousarray(np.flip(v, flips)) for v in vols],
+                                 np.ascontiguousarray(np.flip(tgt, flips)), np.ascontiguousarray(np.flip(wgt, flips)))):
+            vt = [torch.from_numpy(v).to(dev) for v in vv]
+            net.pack_input(ws, vt, (1.0, 1.0, 1.0), origin, s, sym=sym)
+            net.forward(ws, s)
+            net.head_loss(ws, torch.from_numpy(tt).to(dev), torch.from_numpy(ww).to(dev), origin, s, sym=sym)
+            outs.append((net.grads[net.head_offset:].clone(), ws.gr["d0b"].to_dense().clone()))
+        assert torch.equal(outs[0][0], outs[1][0]), code
+        assert torch.equal(outs[0][1], outs[1][1]), code
+    net.status()

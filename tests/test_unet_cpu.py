@@ -139,6 +139,13 @@ def test_focused_crops_hold_a_weighted_voxel_and_stay_in_range():
         if hot.size:
             sub = w[max(o[0], 0):o[0] + crop[0], max(o[1], 0):o[1] + crop[1], max(o[2], 0):o[2] + crop[2]]
             assert sub.any()
+        # in a flipped frame the crop holds a flipped weighted voxel
+        fl = tuple(k for k in range(3) if rng.random() < 0.5)
+        o3 = lc.crop_origin(rng, vd, crop, hot, fl)
+        if hot.size:
+            wf = np.flip(w, fl) if fl else w
+            sub = wf[max(o3[0], 0):o3[0] + crop[0], max(o3[1], 0):o3[1] + crop[1], max(o3[2], 0):o3[2] + crop[2]]
+            assert sub.any()
         o2 = lc.crop_origin(rng, vd, crop)          # unfocused: the same range
         assert all(min(0, vd[k] - crop[k]) <= o2[k] <= max(0, vd[k] - crop[k]) for k in range(3))
 
