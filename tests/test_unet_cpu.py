@@ -171,3 +171,27 @@ def test_every_bulk_copy_stays_inside_the_plane():
         assert g.margin + (g.padded_tiles - 64) + reach + 64 <= g.rows
         # outputs: every written row p < padded_tiles lies inside the plane
         assert g.margin + g.padded_tiles <= g.rows
+
+
+def test_symmetry_codes_are_the_48_grid_symmetries():
+    """symmetry(code): 48 distinct (permutation, flips) pairs, codes 0..7 the flips alone,
+    and numpy's transform of a volume undone by the inverse mapping the library uses."""
+    seen = {lc.symmetry(c) for c in range(48)}
+    assert len(seen) == 48
+    assert all(lc.symmetry(c)[0] == (0, 1, 2) for c in range(8))
+    rng = np.random.default_rng(2)
+    v = rng.random((3, 4, 5))
+    for c in range(48):
+        perm, flips = lc.symmetry(c)
+        u = np.transpose(v, perm)
+        u = np.flip(u, flips) if flips else u
+        assert u.shape == tuple(v.shape[a] for a in perm)
+        # the library's map: U[u] = V[v] with v[perm[k]] = flip_k ? dim - 1 - u_k : u_k
+        for _ in range(5):
+            uu = [int(rng.integers(n)) for n in u.shape]
+            vv = [0, 0, 0]
+            for k in range(3):
+                vv[perm[k]] = v.shape[perm[k]] - 1 - uu[k] if k in flips else uu[k]
+            assert u[tuple(uu)] == v[tuple(vv)]
+    with pytest.raises(ValueError):
+        lc.symmetry(48)
